@@ -1,0 +1,253 @@
+"""Run description and host-side initial state for one 3dmhd instance.
+
+A ``Case`` carries what the reference keeps in 3dmhdparam.h (grid sizes and
+physics switches, 3dmhdparam.h:8-17,25-27,86-107) and in setup()'s ``par[]``
+table (3dmhdset.h:7-24), plus the pieces of a synthetic run the reference
+does not have: a tanh-stretched z grid, a polytropic layer with seeded
+Gaussian temperature noise, a uniform vertical field and a fixed time step.
+
+Arrays follow the reference layout ``f[z][y][x]`` (x fastest, 3dmhddata.h:8)
+on the single global domain with one ghost cell per side:
+``nx = nPx + 2``, ``ny = nPy + 2``, ``nz = nPz + 2``.  z is depth: index 1 is
+the top wall and index nz-2 the bottom wall.
+"""
+from __future__ import annotations
+
+import dataclasses
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Field order of the state, of the checkpoint records (3dmhdio.h:23-33) and of
+# the C-ABI field ids.
+STATE_FIELDS = ("RU", "RV", "RW", "TT", "RO", "BX", "BY", "BZ")
+FLUX_FIELDS = ("FU", "FV", "FW", "FR", "FT", "WW1", "WW2", "WW3")
+ZFIELDS = ("ZRU", "ZRV", "ZRW", "ZTT", "ZRO", "ZBX", "ZBY", "ZBZ")
+
+
+def f32(v: float) -> float:
+    """Value of a C ``float`` literal widened to double (e.g. ``0.2f``)."""
+    return float(np.float32(v))
+
+
+GAMMA_DEFAULT = float(np.float32(5.0) / np.float32(3.0))  # par[53] = 5.0f / 3.0f, 3dmhdset.h:23
+
+
+@dataclass
+class Case:
+    nPx: int
+    nPy: int
+    nPz: int
+    lMag: bool = True
+    lRot: bool = False
+    lShr: bool = False
+    izCon: int = 0          # 0 fixed bottom temperature TB, 1 fixed flux (3dmhdsub.h:842-864)
+    iTCon: int = 0          # 0/1/4 upper temperature condition (3dmhdsub.h:750-810)
+    iBCon: int = 0          # 0: Bz = 0 on both walls (3dmhdsub.h:811-817,865-871)
+    RE: float = 100.0
+    PR: float = 1.0
+    THETA: float = 4.5
+    GRAV: float = 9.0
+    RY: float = 10.0
+    ANG: float = 0.0
+    RM: float = 100.0
+    BETA: float = 2.0
+    TP: float = 0.0
+    xMax: float = 6.0
+    yMax: float = 6.0
+    zMax: float = 2.0
+    GAMMA: float = GAMMA_DEFAULT
+    SFF: float = f32(0.8)   # 3dmhdparam.h:111
+    z_stretch: float = 1.5  # tanh stretch factor; 0 gives the reference's uniform grid
+    TB: float | None = None  # bottom temperature; default is the polytrope's 1 + THETA*zMax
+    seed: int = 0
+    noise: float = 1e-3     # relative Gaussian temperature noise
+    bz0: float = 1e-3       # uniform vertical field in the interior
+    dt: float = 1e-4
+    # decomposition of the multi-rank reference oracle (needs nPEz >= 2, 3dmhdparam.h:20)
+    nPEy: int = 2
+    nPEz: int = 2
+    name: str = ""
+
+    # ---- derived sizes -------------------------------------------------
+    @property
+    def nx(self) -> int:
+        return self.nPx + 2
+
+    @property
+    def ny(self) -> int:
+        return self.nPy + 2
+
+    @property
+    def nz(self) -> int:
+        return self.nPz + 2
+
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def cells(self) -> int:
+        return self.nPx * self.nPy * self.nPz
+
+    @property
+    def tb(self) -> float:
+        return float(self.TB) if self.TB is not None else 1.0 + self.THETA * self.zMax
+
+    @property
+    def nfields(self) -> int:
+        return 8 if self.lMag else 5
+
+    def replace(self, **kw) -> "Case":
+        return dataclasses.replace(self, **kw)
+
+    def to_dict(self) -> dict:
+        return dataclasses.asdict(self)
+
+
+# ---------------------------------------------------------------------------
+# grid metrics
+# ---------------------------------------------------------------------------
+def uniform_metric(n_interior: int, umax: float):
+    """Metric arrays of the uniform grid, as mkGrid(nGrid=0) and the Jacobi
+    routines build them (3dmhdphsic.h:36-41,79-156): dxi/du = 1/umax,
+    d2xi/du2 = 0, DD = (1/(n-1)) / (dxi/du).  Ghost entries repeat the walls."""
+    n = n_interior + 2
+    orx = f32(np.float32(1.0) / np.float32(n_interior - 1))
+    d1 = np.full(n, 1.0 / umax)
+    d2 = np.zeros(n)
+    dd = np.full(n, orx * (1.0 / d1[0]))
+    return d1, d2, dd
+
+
+def tanh_metric(n_interior: int, umax: float, s: float):
+    """Symmetric tanh clustering towards both walls.
+
+    u(xi) = umax/2 * (1 + tanh(s(2xi-1))/tanh(s)),  xi in [0, 1].
+    Returns dxi/du and d2xi/du2 at the n_interior nodes (plus repeated ghost
+    entries) and the DD spacing array used by the CFL estimate.
+    """
+    if s == 0.0:
+        return uniform_metric(n_interior, umax)
+    xi = np.arange(n_interior, dtype=np.float64) / (n_interior - 1)
+    a = s * (2.0 * xi - 1.0)
+    th = np.tanh(a)
+    sech2 = 1.0 - th * th
+    ts = np.tanh(s)
+    du = umax * s * sech2 / ts                        # du/dxi
+    d2u = -4.0 * umax * s * s * th * sech2 / ts       # d2u/dxi2
+    dxidu = 1.0 / du
+    d2xidu2 = -d2u / (du * du * du)
+    orx = 1.0 / (n_interior - 1)
+    dd = orx * (1.0 / dxidu)
+    pad = lambda v: np.concatenate([[v[0]], v, [v[-1]]])
+    return pad(dxidu), pad(d2xidu2), pad(dd)
+
+
+def z_coordinate(case: Case) -> np.ndarray:
+    """Depth of every z index (ghosts repeat the walls)."""
+    n = case.nPz
+    xi = np.arange(n, dtype=np.float64) / (n - 1)
+    if case.z_stretch == 0.0:
+        z = case.zMax * xi
+    else:
+        s = case.z_stretch
+        z = 0.5 * case.zMax * (1.0 + np.tanh(s * (2.0 * xi - 1.0)) / np.tanh(s))
+    return np.concatenate([[z[0]], z, [z[-1]]])
+
+
+@dataclass
+class Metrics:
+    dxxdx: np.ndarray
+    d2xxdx2: np.ndarray
+    DDX: np.ndarray
+    dyydy: np.ndarray
+    d2yydy2: np.ndarray
+    DDY: np.ndarray
+    dzzdz: np.ndarray
+    d2zzdz2: np.ndarray
+    DDZ: np.ndarray
+    RKAPA: np.ndarray
+    DKAPA: np.ndarray
+
+    def arrays(self):
+        return [self.dxxdx, self.d2xxdx2, self.DDX, self.dyydy, self.d2yydy2, self.DDY,
+                self.dzzdz, self.d2zzdz2, self.DDZ, self.RKAPA, self.DKAPA]
+
+
+def metrics(case: Case) -> Metrics:
+    dx = uniform_metric(case.nPx, case.xMax)
+    dy = uniform_metric(case.nPy, case.yMax)
+    dz = tanh_metric(case.nPz, case.zMax, case.z_stretch)
+    # PZP = 0: constant conductivity profile (3dmhd.cpp:478-482)
+    rk = np.ones(case.nz)
+    dk = np.zeros(case.nz)
+    return Metrics(*dx, *dy, *dz, rk, dk)
+
+
+# ---------------------------------------------------------------------------
+# initial state
+# ---------------------------------------------------------------------------
+def periodic_fill(a: np.ndarray) -> None:
+    """x/y ghosts become periodic images (final semantics of comm_mpi,
+    3dmhdmpi.h:32-143, on one domain): index 0 <- n-2, index n-1 <- 1."""
+    a[:, 0, :] = a[:, -2, :]
+    a[:, -1, :] = a[:, 1, :]
+    a[:, :, 0] = a[:, :, -2]
+    a[:, :, -1] = a[:, :, 1]
+
+
+def initial_state(case: Case) -> dict[str, np.ndarray]:
+    """Polytrope T = 1 + THETA*z, rho = T**m with m = GRAV/THETA - 1, seeded
+    multiplicative Gaussian temperature noise on the interior, a uniform Bz on
+    interior planes (zero on the walls, where iBCon=0 pins it), zero momenta.
+    The z ghost planes hold the noise-free wall values."""
+    nz, ny, nx = case.shape
+    z = z_coordinate(case)
+    m = case.GRAV / case.THETA - 1.0
+    T1 = 1.0 + case.THETA * z
+    R1 = T1 ** m
+    TT = np.broadcast_to(T1[:, None, None], case.shape).copy()
+    RO = np.broadcast_to(R1[:, None, None], case.shape).copy()
+    rng = np.random.default_rng(case.seed)
+    noise = rng.standard_normal((case.nPz, case.nPy, case.nPx))
+    TT[1:-1, 1:-1, 1:-1] *= 1.0 + case.noise * noise
+    st = {k: np.zeros(case.shape) for k in STATE_FIELDS}
+    st["TT"] = TT
+    st["RO"] = RO
+    if case.lMag:
+        st["BZ"][2:-2, :, :] = case.bz0
+    if case.lShr:
+        # moving-wall shear runs start from the wall velocities BCON imposes
+        # (3dmhdsub.h:729-734,821-826): rho*v = +rho on top, -rho at the bottom
+        st["RV"][1] = RO[1]
+        st["RV"][-2] = -RO[-2]
+    for k in STATE_FIELDS:
+        periodic_fill(st[k])
+    return st
+
+
+def small_cases() -> dict[str, Case]:
+    """Small switch-coverage cases shared by the golden fixtures and the
+    parity tests (grid sizes the CPU oracle finishes in well under a second)."""
+    base = dict(nPx=12, nPy=8, nPz=8, nPEy=2, nPEz=2, seed=7, noise=1e-2, bz0=1e-2, dt=2e-4)
+    return {
+        "mhd_fixedT": Case(name="mhd_fixedT", **base),
+        "mhd_rot_shr": Case(name="mhd_rot_shr", lRot=True, lShr=True, **base),
+        "hydro_default_bc": Case(name="hydro_default_bc", lMag=False, izCon=1, iTCon=4, TP=f32(0.1), **base),
+        "mhd_rot_flux": Case(name="mhd_rot_flux", lRot=True, ANG=0.3, izCon=1, iTCon=1, **base),
+        "hydro_shr": Case(name="hydro_shr", lMag=False, lShr=True, izCon=0, iTCon=4, TP=f32(0.1), **base),
+    }
+
+
+def config0() -> Case:
+    """64x64x32 plain FP64 MHD run: polytrope index 1 (THETA=4.5, GRAV=9,
+    density contrast 10), tanh z grid (1.5), noise 1e-3, Bz=1e-3, 1/Re=1e-2,
+    Pr=1, Pm=1, dt=1e-4, 100 steps; the oracle runs it on 2x2 ranks."""
+    return Case(name="config0_64x64x32", nPx=64, nPy=64, nPz=32, lMag=True, seed=1, nPEy=2, nPEz=2)
+
+
+def config1() -> Case:
+    """512x512x256 FP64 MHD with rotation 0.1 about z and the shear switch."""
+    return Case(name="config1_512x512x256", nPx=512, nPy=512, nPz=256, lMag=True, lRot=True, lShr=True,
+                RY=10.0, ANG=0.0, seed=1, nPEy=4, nPEz=4)

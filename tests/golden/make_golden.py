@@ -1,0 +1,90 @@
+"""Generate the golden fixtures from the reference 3dmhd code itself.
+
+Run in a checkout that has the reference sources (default /root/reference,
+override with MHD_REFERENCE_DIR):
+
+    python tests/golden/make_golden.py
+
+For every small switch-coverage case (mhd_gb300.case.small_cases) it builds
+the reference with oracle/refcase.py (2 x 2 forked MPI ranks), feeds it the
+seeded initial state and stores, as <case>.npz:
+  in_*      the input state and metric arrays (so the fixture does not depend
+            on this host's libm when it is replayed elsewhere)
+  flux_*    the right-hand sides after one fluxes() call (interior only)
+  steps3_*  the full state (ghosts included) after 3 fixed-dt RK3 steps
+  cfl2_*    the state after 2 steps of the reference step() with its CFL dt,
+            and cfl2_dt the two time steps (two cases only)
+plus config0_digest.json: SHA-256 digests of the 64x64x32 MHD run of the
+plain-method configuration after 100 fixed-dt steps (too large to store).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(REPO / "oracle"))
+sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
+
+import refcase  # noqa: E402
+from mhd_gb300.case import FLUX_FIELDS, STATE_FIELDS, config0, initial_state, metrics, small_cases  # noqa: E402
+
+METRIC_NAMES = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
+CFL_CASES = ("mhd_fixedT", "hydro_default_bc")
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def main() -> None:
+    if not refcase.reference_available():
+        raise SystemExit(f"reference sources not found under {refcase.REF_DIR}")
+    manifest = {}
+    for name, case in small_cases().items():
+        st = initial_state(case)
+        m = metrics(case)
+        out = {}
+        for k in STATE_FIELDS:
+            out["in_" + k] = st[k]
+        for k, a in zip(METRIC_NAMES, m.arrays()):
+            out["in_" + k] = a
+        r = refcase.run(case, st, "fluxes", 0)
+        for k in FLUX_FIELDS:
+            out["flux_" + k] = r[k][1:-1, 1:-1, 1:-1]
+        r = refcase.run(case, st, "steps", 3)
+        for k in STATE_FIELDS:
+            out["steps3_" + k] = r[k]
+        if name in CFL_CASES:
+            r = refcase.run(case, st, "cfl", 2)
+            for k in STATE_FIELDS:
+                out["cfl2_" + k] = r[k]
+            out["cfl2_dt"] = r["dt_hist"]
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+        manifest[name] = case.to_dict()
+        print("wrote", name)
+    (HERE / "cases.json").write_text(json.dumps(manifest, indent=1, sort_keys=True))
+
+    c0 = config0()
+    st = initial_state(c0)
+    r = refcase.run(c0, st, "steps", 100)
+    digest = {
+        "case": c0.to_dict(),
+        "steps": 100,
+        "reference_ranks": c0.nPEy * c0.nPEz,
+        "input_sha256": {k: sha(st[k]) for k in STATE_FIELDS},
+        "output_sha256": {k: sha(r[k]) for k in STATE_FIELDS},
+        "output_interior_absmax": {k: float(np.abs(r[k][1:-1, 1:-1, 1:-1]).max()) for k in STATE_FIELDS},
+        "TIMT": r["TIMT"],
+    }
+    (HERE / "config0_digest.json").write_text(json.dumps(digest, indent=1, sort_keys=True))
+    print("wrote config0_digest.json")
+
+
+if __name__ == "__main__":
+    main()

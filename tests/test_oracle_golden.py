@@ -1,0 +1,80 @@
+"""The CPU oracle (oracle/mhd_oracle.c) against fixtures produced by the
+reference 3dmhd code itself (tests/golden/make_golden.py): bit-exact."""
+import hashlib
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_case_names, load_golden
+from mhd_gb300.case import FLUX_FIELDS, STATE_FIELDS, config0, initial_state
+
+import oracle
+
+METRIC_NAMES = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
+
+
+def oracle_from_fixture(case, g):
+    sim = oracle.OracleSim(case)
+    # replay the fixture's own metric arrays and input state
+    for n, a in zip(METRIC_NAMES, sim._metric_arrays):
+        a[...] = g["in_" + n]
+    sim.load({k: g["in_" + k] for k in STATE_FIELDS})
+    sim.communicate()
+    return sim
+
+
+@pytest.mark.parametrize("name", golden_case_names())
+def test_fluxes_bit_exact(name):
+    case, g = load_golden(name)
+    sim = oracle_from_fixture(case, g)
+    sim.fluxes()
+    names = FLUX_FIELDS if case.lMag else FLUX_FIELDS[:5]
+    for k in names:
+        got = sim.arr[k][1:-1, 1:-1, 1:-1]
+        assert np.array_equal(got, g["flux_" + k]), k
+
+
+@pytest.mark.parametrize("name", golden_case_names())
+def test_three_steps_bit_exact(name):
+    case, g = load_golden(name)
+    sim = oracle_from_fixture(case, g)
+    sim.steps(3)
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(sim.arr[k], g["steps3_" + k]), k
+
+
+@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc"])
+def test_cfl_steps_bit_exact(name):
+    case, g = load_golden(name)
+    sim = oracle_from_fixture(case, g)
+    dts = sim.steps(2, dt=0.0)
+    assert np.array_equal(dts, g["cfl2_dt"])
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(sim.arr[k], g["cfl2_" + k]), k
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def test_config0_100_steps_digest():
+    """64x64x32 MHD, 100 fixed-dt steps: the oracle's final state hashes to
+    the reference's (4 ranks)."""
+    d = json.loads((GOLDEN / "config0_digest.json").read_text())
+    case = config0()
+    st = initial_state(case)
+    if any(_sha(st[k]) != d["input_sha256"][k] for k in STATE_FIELDS):
+        pytest.skip("this host's libm generates a different seeded input; digest not comparable")
+    sim = oracle.OracleSim(case, st, nthreads=8)
+    sim.communicate()
+    sim.steps(d["steps"])
+    for k in STATE_FIELDS:
+        assert _sha(sim.arr[k]) == d["output_sha256"][k], k
+
+
+def test_unsupported_wall_condition_is_rejected():
+    case, g = load_golden("mhd_fixedT")
+    sim = oracle_from_fixture(case.replace(TP=0.1), g)
+    with pytest.raises(ValueError):
+        sim.BCON()
