@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark of the 3dmhd hot path on GB300: cell-RK3-updates/s.
+
+Workload (default): the plain-method FP64 configuration at 512x512x256 with
+lMag, lRot (rotation 0.1 about z) and lShr on, polytropic layer with seeded
+Gaussian temperature noise, fixed dt = 1e-4.  One "step" is one full Wray RK3
+step (three fused substages + wall conditions + ghost fill) over the whole
+grid.  The state (about 13 GB) is far larger than L2, so no flush is needed.
+
+  value      interior cells x steps / device time (CUDA events on the
+             context's stream), inputs resident in HBM
+  e2e        the same metric through the C ABI with pinned HOST buffers:
+             every step uploads the state, steps once and downloads it
+  roofline   the fused substage kernel: algorithmic HBM bytes per launch over
+             its average duration (events around each launch), against the
+             measured HBM copy peak; plus the FP64 pipe, which binds first
+  cpu_baseline  the CPU oracle (a restatement of the reference's own code,
+             bit-exact with it) on a bounded slab of the same workload
+
+`--impl reference` times the reference's CPU implementation of the path
+(the oracle port; the reference binary itself cannot be built on the GPU host)
+with all host threads on the same metric and configuration.
+
+Multi-GPU (torchrun): replicas only -- every rank steps its own instance;
+`value` is the sum over ranks of cells x steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
+
+from mhd_gb300 import abi  # noqa: E402
+from mhd_gb300.case import STATE_FIELDS, config0, config1, initial_state  # noqa: E402
+
+METRIC = "cell-RK3-updates/s"
+# Algorithmic HBM traffic of the fused FP64 path per interior cell and RK3
+# step: substage 1 reads U and writes U', Z' (24 doubles), substage 2 reads U,
+# Z and writes U', Z' (32), substage 3 reads U, Z and writes U' (24) for the
+# 8 MHD fields = 640 B; with lShr the persistent FT adds a read and a write
+# per substage (48 B).  Hydro-only (5 fields): 400 B.
+def algorithmic_bytes_per_cell_step(case) -> float:
+    nf = case.nfields
+    b = 80.0 * nf
+    if case.lShr:
+        b += 3 * 16.0
+    return b
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sms, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sms), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def case_for(name: str):
+    c1 = config1()
+    # "mid": the same physics at 256x256x128 (about 1.6 GB of state, larger
+    # than L2), the size used for ncu captures
+    mid = c1.replace(nPx=256, nPy=256, nPz=128, name="config1_physics_256x256x128")
+    return {"config1": c1, "config0": config0(), "mid": mid}[name]
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restating the reference code; checker only)
+# ---------------------------------------------------------------------------
+def cpu_sample_case(case):
+    """A slab of the workload: same horizontal grid and physics, 16 interior
+    z planes; the per-cell work of the RK3 step is the same."""
+    return case.replace(nPz=16, name=case.name + "_slab16")
+
+
+def cpu_baseline(case, target_s: float = 12.0, threads: int | None = None) -> dict:
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    sc = cpu_sample_case(case)
+    st = initial_state(sc)
+    o = oracle.OracleSim(sc, st, nthreads=threads)
+    o.communicate()
+    t = time.perf_counter()
+    o.steps(1)
+    t1 = time.perf_counter() - t
+    n = max(1, min(50, int(target_s / max(t1, 1e-3))))
+    t = time.perf_counter()
+    o.steps(n)
+    secs = time.perf_counter() - t
+    return {"value": sc.cells * n / secs, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{sc.nPx}x{sc.nPy}x{sc.nPz} slab of the workload (same physics), {n} RK3 steps after 1 warm-up, "
+                      f"oracle/mhd_oracle.c with OpenMP over {threads} threads, {secs:.1f} s"}
+
+
+def run_reference(args, dist: Dist) -> None:
+    if dist.rank != 0:
+        return
+    case = case_for(args.config)
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    threads = os.cpu_count() or 1
+    sc = cpu_sample_case(case)
+    st = initial_state(sc)
+    o = oracle.OracleSim(sc, st, nthreads=threads)
+    o.communicate()
+    o.steps(max(1, args.warmup))
+    t = time.perf_counter()
+    o.steps(args.steps)
+    secs = time.perf_counter() - t
+    value = sc.cells * args.steps / secs
+    sample = (f"each step: one RK3 step of a {sc.nPx}x{sc.nPy}x{sc.nPz} slab of the {case.name} workload "
+              f"(same physics), oracle/mhd_oracle.c (bit-exact restatement of the reference) on {threads} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(case, args),
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(case, args) -> dict:
+    return {"workload": f"{case.name}: plain method FP64, {case.nPx}x{case.nPy}x{case.nPz}, "
+                        f"lMag={case.lMag} lRot={case.lRot} lShr={case.lShr}, fixed dt={case.dt}",
+            "grid": [case.nPx, case.nPy, case.nPz], "cells": case.cells, "precision": "fp64",
+            "path": "fused", "parallelism": f"replicas x{args.gpus}",
+            "l2": "no flush: state of 24 fields x 545 MB is far larger than the 129 MB L2"}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, dist: Dist) -> None:
+    from mhd_gb300.sim import Simulation
+    L = abi.load()
+    abi.check(L.mhd_set_device(dist.local))
+    case = case_for(args.config)
+    st = initial_state(case)
+    sim = Simulation(case, path="fused")
+    sim.upload_state(st)
+    sim.communicate()
+    for _ in range(args.warmup):
+        sim.step(case.dt)
+    sim.sync()
+
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    sim.sync()
+    clocks.start()
+    sim.profile(True)
+    sim.timer_start()
+    for _ in range(args.steps):
+        sim.step(case.dt)
+    ms = sim.timer_stop()
+    sub_ms, launches = sim.profile_read()
+    sim.profile(False)
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = dist.world * case.cells * args.steps / (ms_max / 1e3)
+
+    # roofline of the fused substage kernel
+    bytes_cell_step = algorithmic_bytes_per_cell_step(case)
+    per_launch_bytes = case.cells * bytes_cell_step / 3.0
+    avg_launch_s = (sub_ms / 1e3) / max(launches, 1)
+    achieved_gbs = per_launch_bytes / avg_launch_s / 1e9
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    fp64_peak = C.c_double(0.0)
+    abi.check(L.mhd_fp64_peak(C.byref(fp64_peak)))
+    fp64_flops_cell_substage = FP64_FLOPS_PER_CELL_SUBSTAGE.get((case.lMag, case.lRot, case.lShr))
+
+    # end to end through the C ABI with pinned host buffers
+    nf = case.nfields
+    ncell = int(np.prod(case.shape))
+    nbytes = nf * ncell * 8
+    hp = C.c_void_p()
+    abi.check(L.mhd_host_alloc(nbytes, C.byref(hp)))
+    host = np.ctypeslib.as_array(C.cast(hp, C.POINTER(C.c_double)), shape=(nf * ncell,))
+    for j, k in enumerate(STATE_FIELDS[:nf]):
+        host[j * ncell:(j + 1) * ncell] = st[k].ravel()
+    ptr = C.cast(hp, C.POINTER(C.c_double))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, args.e2e_steps))
+    e2e_s = float("nan")
+    if e2e_steps:
+        abi.check(L.mhd_upload_state(sim.ctx, ptr))
+        sim.step(case.dt)
+        abi.check(L.mhd_download_state(sim.ctx, ptr))
+        dist.barrier()
+        t = time.perf_counter()
+        for _ in range(e2e_steps):
+            abi.check(L.mhd_upload_state(sim.ctx, ptr))
+            sim.step(case.dt)
+            abi.check(L.mhd_download_state(sim.ctx, ptr))
+        e2e_s = dist.max(time.perf_counter() - t)
+    e2e_value = dist.world * case.cells * e2e_steps / e2e_s if e2e_steps else None
+    L.mhd_host_free(hp)
+    sim.close()
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(case)
+
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded polytrope + Gaussian T noise)",
+        "config": workload_config(case, args),
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps if e2e_steps else None,
+                "path": "mhd_upload_state + mhd_step + mhd_download_state, pinned host memory"},
+        "gpu_launches": 6 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": TRAFFIC_PER_LAUNCH.get(args.config),
+                     "kernel": "k_substage (fused RK3 substage)", "peak_source": f"{peak_src} hbm_gbs",
+                     "algorithmic_bytes_per_cell_step": bytes_cell_step,
+                     "avg_launch_ms": 1e3 * avg_launch_s, "launches": launches},
+        "fp64": {"peak_tflops_measured": fp64_peak.value,
+                 "flops_per_cell_substage": fp64_flops_cell_substage,
+                 "achieved_tflops": (fp64_flops_cell_substage * case.cells / avg_launch_s / 1e12
+                                     if fp64_flops_cell_substage else None),
+                 "frac": (fp64_flops_cell_substage * case.cells / avg_launch_s / 1e12 / fp64_peak.value
+                          if fp64_flops_cell_substage and fp64_peak.value > 0 else None),
+                 "note": "the FP64 pipe, not HBM, bounds the fused FP64 kernel on GB300"},
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+# FP64 flops per interior cell per substage of the fused kernel, from ncu's
+# dadd/dmul/dfma instruction counts (see profiles/); None until measured.
+FP64_FLOPS_PER_CELL_SUBSTAGE: dict = {}
+# dram__bytes_read.sum + dram__bytes_write.sum per k_substage launch, from ncu.
+TRAFFIC_PER_LAUNCH: dict = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=["config1", "config0", "mid"], default="config1")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

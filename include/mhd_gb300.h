@@ -1,0 +1,186 @@
+/*
+ * mhd_gb300.h -- C ABI of the GB300-native 3dmhd hot path.
+ *
+ * Drop-in replacement for the reference's per-timestep functions
+ * (thu-scc/Rast-3dmhd-cpp).  A driver that today calls
+ *     step()        3dmhdsub.h:31      (CFL dt + three RK3 substages)
+ *     fluxes()      3dmhdsub.h:18,194  (right-hand sides)
+ *     step_block_ZETA0 / ZETA / GAM    3dmhdsub.h:20-22,155-192
+ *     BCON()        3dmhdsub.h:19,720  (z-wall conditions)
+ *     communicate() 3dmhdmpi.h:11      (ghost exchange)
+ * calls the mhd_* function of the same role instead.  Plain C types only.
+ *
+ * Layout: every field is a host array double[nz][ny][nx] with x fastest
+ * and one ghost cell on each side, nx = nPx+2, ny = nPy+2, nz = nPz+2, as
+ * the reference's `data` type (3dmhddata.h:8) on one global domain.  z is
+ * depth: index 1 is the top wall, nz-2 the bottom wall, 0 and nz-1 the wall
+ * ghost planes.
+ *
+ * Every function returns an int status (MHD_OK = 0, negative on error) and
+ * never exits the process (the reference calls exit_err, 3dmhdutils.h:39-43).
+ * mhd_last_error() gives the text of the last failure of a context.
+ * A context is driven from one host thread; work is queued on the context's
+ * CUDA stream and is asynchronous until mhd_sync() or a download.
+ */
+#ifndef MHD_GB300_H_
+#define MHD_GB300_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MHD_ABI_VERSION 1
+
+/* status codes */
+#define MHD_OK 0
+#define MHD_ERR_INVALID (-1)      /* bad argument or size */
+#define MHD_ERR_UNSUPPORTED (-2)  /* switch / boundary combination not built */
+#define MHD_ERR_CUDA (-3)         /* CUDA runtime error (text in mhd_last_error) */
+#define MHD_ERR_NUMERIC (-4)      /* non-finite or non-positive rho/T seen by a reduction */
+#define MHD_ERR_DT_TOO_SMALL (-5) /* CFL dt below 1e-8 (3dmhd.cpp:292-331) */
+#define MHD_ERR_NOMEM (-6)        /* device allocation failed */
+#define MHD_ERR_TIMEOUT (-7)      /* a bounded device wait gave up */
+
+/* physics switches (3dmhdparam.h:8-17) */
+#define MHD_SW_LROT 0x1u
+#define MHD_SW_LMAG 0x2u
+#define MHD_SW_LPOT 0x4u /* no effect: the reference never reads lPot */
+#define MHD_SW_LREM 0x8u /* not supported: MHD_ERR_UNSUPPORTED */
+#define MHD_SW_LSHR 0x10u
+
+/* storage precision of the state */
+#define MHD_PREC_FP64 0
+#define MHD_PREC_FP32 1 /* fields stored and stenciled in FP32, RK register and EOS in FP64 */
+
+/* kernel path of mhd_step / mhd_steps */
+#define MHD_PATH_FUSED 0  /* one fused pass per RK3 substage (FMA contraction on) */
+#define MHD_PATH_PARITY 1 /* the unfused sequence below, bit-exact with the reference */
+
+/* field ids: state 0-7 (dump record order, 3dmhdio.h:23-33), right-hand
+ * sides 8-15, RK register 16-23 */
+enum {
+    MHD_RU = 0, MHD_RV, MHD_RW, MHD_TT, MHD_RO, MHD_BX, MHD_BY, MHD_BZ,
+    MHD_FU = 8, MHD_FV, MHD_FW, MHD_FR, MHD_FT, MHD_WW1, MHD_WW2, MHD_WW3,
+    MHD_ZRU = 16, MHD_ZRV, MHD_ZRW, MHD_ZTT, MHD_ZRO, MHD_ZBX, MHD_ZBY, MHD_ZBZ,
+    MHD_NFIELDS = 24
+};
+
+/* Run description: sizes, switches (3dmhdparam.h), the par[] run table
+ * (3dmhdset.h:7-24) and the metric arrays (3dmhddata.h:21-23, built by
+ * x/y/zJacobi, 3dmhdphsic.h:79-156).  Metric pointers are host arrays of
+ * nx / ny / nz doubles, copied at mhd_create. */
+typedef struct mhd_params {
+    int nPx, nPy, nPz;
+    unsigned switches;
+    int ixCon, iyCon, izCon, iTCon, iBCon;
+    int precision;
+    int path;
+    int reserved_i[5];
+    double RE, PR, THETA, GRAV, RY, ANG, RM, BETA, TP, GAMMA, SFF, TB;
+    double reserved_d[4];
+    const double *dxxdx, *d2xxdx2, *DDX;
+    const double *dyydy, *d2yydy2, *DDY;
+    const double *dzzdz, *d2zzdz2, *DDZ;
+    const double *RKAPA, *DKAPA;
+} mhd_params;
+
+/* Derived scalars exactly as set() and main() compute them
+ * (3dmhd.cpp:144-145,354-369,432-459), single-precision literals included. */
+typedef struct mhd_constants {
+    double C13, C23, C43, GAM1, GAM2, GAM3, ZETA1, ZETA2;
+    double hx, h2x, hy, h2y, hz, h2z;
+    double REPR, ORE, ORM, OBETA, OMX, OMZ, CV, OCV;
+} mhd_constants;
+
+/* Per-step results and diagnostics (the reference prints DT and UMACH,
+ * 3dmhd.cpp:290, 3dmhdio.h:229-239; the conserved totals are new). */
+typedef struct mhd_diag {
+    double dt;           /* time step used by the last step */
+    double umach;        /* max Mach number of the state the CFL step saw */
+    double timt;         /* simulation time (TIMT) */
+    double total_mass;   /* sum of rho over interior cells x cell volume */
+    double total_energy; /* sum of |rho u|^2/(2 rho) + CV rho T + OBETA |B|^2/2, x cell volume */
+    double max_divb;     /* max |Dx Bx + Dy By + Dz Bz| over non-wall interior cells */
+    long long nit;       /* completed steps (nIt) */
+    int flags;           /* bit 0: non-finite value, bit 1: rho <= 0, bit 2: T <= 0 */
+    int reserved;
+} mhd_diag;
+
+typedef struct mhd_ctx mhd_ctx;
+
+/* ---- lifetime -------------------------------------------------------- */
+/* Replaces the static globals of 3dmhd.cpp:29-39 with device buffers owned
+ * by the context.  `stream` is a cudaStream_t (NULL: the context creates
+ * its own non-blocking stream). */
+int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out);
+int mhd_destroy(mhd_ctx* ctx);
+int mhd_get_constants(const mhd_ctx* ctx, mhd_constants* out);
+/* The same derivation without a context or a GPU (host arithmetic only). */
+int mhd_compute_constants(const mhd_params* params, mhd_constants* out);
+/* Bytes of device memory the context holds. */
+int mhd_device_bytes(const mhd_ctx* ctx, size_t* out);
+const char* mhd_last_error(const mhd_ctx* ctx);
+const char* mhd_status_string(int status);
+
+/* ---- state transfer (dump / restart, 3dmhdio.h:20-72) ----------------- */
+/* Copy one whole field (ghosts included) host <-> device.  A download
+ * synchronises the context's stream. */
+int mhd_upload(mhd_ctx* ctx, int field, const double* host);
+int mhd_download(mhd_ctx* ctx, int field, double* host);
+/* All nfields state fields (5 without lMag, else 8) from / to one
+ * contiguous host block of nfields * nz*ny*nx doubles in field-id order. */
+int mhd_upload_state(mhd_ctx* ctx, const double* host);
+int mhd_download_state(mhd_ctx* ctx, double* host);
+/* Simulation time and step counter (TIMT, nIt). */
+int mhd_set_time(mhd_ctx* ctx, double timt, long long nit);
+
+/* ---- unfused parity ABI: one call per reference function ---------------- */
+int mhd_fluxes(mhd_ctx* ctx);                   /* fluxes(FORRANGE), 3dmhdsub.h:194-696 */
+int mhd_rk_zeta0(mhd_ctx* ctx);                 /* step_block_ZETA0, 3dmhdsub.h:155-166 */
+int mhd_rk_zeta(mhd_ctx* ctx, double coef);     /* step_block_ZETA(coef), 3dmhdsub.h:168-179 */
+int mhd_rk_gam(mhd_ctx* ctx, double coef);      /* step_block_GAM(coef), 3dmhdsub.h:181-192 */
+int mhd_bcon(mhd_ctx* ctx, double timt);        /* BCON(FORRANGE), 3dmhdsub.h:720-873 */
+int mhd_communicate(mhd_ctx* ctx);              /* communicate(), 3dmhdmpi.h:11-143 */
+/* CFL time step of step() (3dmhdsub.h:36-106); blocks until known. */
+int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach);
+
+/* ---- fused time stepping ------------------------------------------------ */
+/* One RK3 step, replacing step() (3dmhdsub.h:31-153).  dt > 0: fixed step;
+ * dt <= 0: the reference's CFL step (then the call blocks for the dt).
+ * `out` (may be NULL) receives dt/umach/timt/nit. */
+int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out);
+/* n fixed-dt steps queued without host synchronisation. */
+int mhd_steps(mhd_ctx* ctx, int n, double dt);
+/* Mass, energy, max|div B| and sanity flags of the current state (blocks). */
+int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
+int mhd_sync(mhd_ctx* ctx);
+
+/* ---- device selection and timing ---------------------------------------- */
+/* Make `device` current for this thread's later mhd_* calls (one process per
+ * GPU, e.g. under torchrun). */
+int mhd_set_device(int device);
+/* CUDA events on the context's stream: start, then stop returns the elapsed
+ * milliseconds (waits for the stop event). */
+int mhd_timer_start(mhd_ctx* ctx);
+int mhd_timer_stop(mhd_ctx* ctx, double* ms);
+/* enable != 0: bracket every fused-substage kernel launch with events;
+ * mhd_profile_read sums their durations (ms) and counts the launches since
+ * the last enable, after waiting for them. */
+int mhd_profile(mhd_ctx* ctx, int enable);
+int mhd_profile_read(mhd_ctx* ctx, double* substage_ms, long long* launches);
+
+/* FP64 FMA throughput of the current device in TFLOP/s, measured with
+ * independent DFMA chains (the roof of the FP64 path on GB300). */
+int mhd_fp64_peak(double* tflops);
+
+/* ---- pinned host memory helpers (for callers without a CUDA toolkit) --- */
+int mhd_host_alloc(size_t bytes, void** out);
+int mhd_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

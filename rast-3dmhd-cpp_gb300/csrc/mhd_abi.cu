@@ -1,0 +1,630 @@
+// mhd_abi.cu -- host side of the C ABI declared in include/mhd_gb300.h.
+//
+// A context replaces the reference's static globals (3dmhd.cpp:29-39) by
+// device buffers:
+//   U[2]   two copies of the state (RU RV RW TT RO BX BY BZ), ping-ponged by
+//          the fused path, each field a full [nz][ny][nx] array with ghosts
+//   Z      the RK register (ZRU ... ZBZ)
+//   F      the right-hand sides (FU FV FW FR FT WW1 WW2 WW3); the fused path
+//          only keeps FT, and only with lShr (where the reference carries it
+//          across substages)
+//   S      scratch of the unfused path: p = rho*T and the velocities
+// Buffers that a call sequence never needs are allocated on first use.
+#include "../../include/mhd_gb300.h"
+#include "mhd_common.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace mhd;
+
+struct mhd_ctx {
+    mhd_params prm{};
+    mhd_constants k{};
+    Grid g{};
+    Consts c{};
+    Coefs coef{};
+    unsigned sw = 0;
+    int nf = 5;
+    size_t ncell = 0;  // nx*ny*nz
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double* d_metric = nullptr;  // 11 metric arrays + 9 coefficient arrays
+    double* U[2] = {nullptr, nullptr};
+    int cur = 0;
+    double* Zb = nullptr;
+    double* Fb = nullptr;
+    double* Sb = nullptr;
+    double* red = nullptr;   // reduction partials
+    double* d_out = nullptr; // 8 doubles of reduction results
+    double* h_out = nullptr; // pinned mirror of d_out
+    int red_blocks = 0;
+    bool ghosts_synced = false;  // z ghost planes of U[1-cur] match U[cur]
+    double timt = 0.0;
+    long long nit = 0;
+    double last_dt = 0.0, last_umach = 0.0;
+    size_t bytes = 0;
+    std::string err;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;  // pairs around each substage launch
+    size_t prof_used = 0;
+};
+
+namespace {
+
+int fail(mhd_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(mhd_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, MHD_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+size_t field_bytes(const mhd_ctx* c) { return c->ncell * sizeof(double); }
+
+int alloc_block(mhd_ctx* ctx, double** p, int nfields) {
+    if (*p) return MHD_OK;
+    const size_t b = field_bytes(ctx) * (size_t)nfields;
+    cudaError_t e = cudaMalloc(p, b);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(ctx, MHD_ERR_NOMEM, "device allocation of " + std::to_string(b) + " bytes failed");
+    }
+    ctx->bytes += b;
+    e = cudaMemsetAsync(*p, 0, b, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync");
+    return MHD_OK;
+}
+
+Fields8 fields_of(const mhd_ctx* c, double* base) {
+    Fields8 f{};
+    for (int k = 0; k < 8; k++) f.p[k] = base ? base + (size_t)k * c->ncell : nullptr;
+    return f;
+}
+
+// Derived scalars exactly as set() and main() compute them: the literals of
+// 3dmhd.cpp:354-369 are single precision; 3dmhd.cpp:432-438,451-459; 144-145.
+void compute_constants(const mhd_params& p, mhd_constants& k) {
+    k.C13 = 1.0f / 3.0f;
+    k.C23 = 2.0f * k.C13;
+    k.C43 = 4.0f * k.C13;
+    k.GAM1 = 8.0f / 15.0f;
+    k.GAM2 = 5.0f / 12.0f;
+    k.GAM3 = 3.0f / 4.0f;
+    k.ZETA1 = -17.0f / 60.0f;
+    k.ZETA2 = -5.0f / 12.0f;
+    k.hx = 0.5f * float(p.nPx - 1);
+    k.h2x = float(p.nPx - 1) * float(p.nPx - 1);
+    k.hy = 0.5f * float(p.nPy - 1);
+    k.h2y = float(p.nPy - 1) * float(p.nPy - 1);
+    k.hz = 0.5f * float(p.nPz - 1);
+    k.h2z = float(p.nPz - 1) * float(p.nPz - 1);
+    if (p.switches & MHD_SW_LROT) {
+        k.OMX = std::sin(p.ANG) / p.RY;
+        k.OMZ = std::cos(p.ANG) / p.RY;
+    } else {
+        k.OMX = 0.0f;
+        k.OMZ = 0.0f;
+    }
+    k.REPR = p.RE * p.PR;
+    k.ORE = 1.0f / p.RE;
+    k.ORM = 1.0f / p.RM;
+    k.OBETA = 2.0f / p.BETA;
+    k.CV = 1.0f / (p.GAMMA - 1.0f);
+    k.OCV = 1.0f / k.CV;
+}
+
+int validate(const mhd_params* p, std::string& why) {
+    if (!p) return why = "params is NULL", MHD_ERR_INVALID;
+    if (p->nPx < 2 || p->nPy < 2) return why = "nPx and nPy must be >= 2", MHD_ERR_INVALID;
+    if (p->nPz < 4) return why = "nPz must be >= 4 (one-sided wall stencils reach 4 planes)", MHD_ERR_INVALID;
+    const double cells = (double)(p->nPx + 2) * (p->nPy + 2) * (p->nPz + 2);
+    if (cells > 2.0e9) return why = "grid too large for 32-bit plane indexing", MHD_ERR_INVALID;
+    if (p->ixCon != 0 || p->iyCon != 0) return why = "only periodic horizontal boundaries (ixCon=iyCon=0) exist in the reference", MHD_ERR_UNSUPPORTED;
+    if (p->switches & MHD_SW_LREM) return why = "lRem (Rempel relaxation) is not built", MHD_ERR_UNSUPPORTED;
+    if (p->izCon != 0 && p->izCon != 1) return why = "izCon must be 0 or 1", MHD_ERR_UNSUPPORTED;
+    if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 4) return why = "iTCon must be 0, 1 or 4", MHD_ERR_UNSUPPORTED;
+    if ((p->iTCon == 0 || p->iTCon == 1) && p->TP != 0.0)
+        return why = "the plume upper boundary (TP != 0 with iTCon 0/1) is not built", MHD_ERR_UNSUPPORTED;
+    if (p->iBCon != 0) return why = "iBCon must be 0", MHD_ERR_UNSUPPORTED;
+    if (p->precision != MHD_PREC_FP64) return why = "this context type stores FP64 state", MHD_ERR_UNSUPPORTED;
+    if (p->path != MHD_PATH_FUSED && p->path != MHD_PATH_PARITY) return why = "unknown kernel path", MHD_ERR_INVALID;
+    if (!(p->RE > 0) || !(p->RM > 0) || !(p->BETA > 0) || !(p->PR > 0) || !(p->GAMMA > 1))
+        return why = "RE, RM, BETA, PR must be > 0 and GAMMA > 1", MHD_ERR_INVALID;
+    const double* arrs[11] = {p->dxxdx, p->d2xxdx2, p->DDX, p->dyydy, p->d2yydy2, p->DDY,
+                              p->dzzdz, p->d2zzdz2, p->DDZ, p->RKAPA, p->DKAPA};
+    for (int i = 0; i < 11; i++)
+        if (!arrs[i]) return why = "a metric array pointer is NULL", MHD_ERR_INVALID;
+    return MHD_OK;
+}
+
+int ensure_u1(mhd_ctx* ctx) {
+    if (!ctx->U[1]) {
+        int rc = alloc_block(ctx, &ctx->U[1], 8);
+        if (rc) return rc;
+        ctx->ghosts_synced = false;
+    }
+    return MHD_OK;
+}
+
+// The fused path writes every cell of U[1-cur] except the z ghost planes:
+// copy those from U[cur] when they may differ.
+int sync_zghosts(mhd_ctx* ctx) {
+    if (ctx->ghosts_synced) return MHD_OK;
+    const size_t plane = (size_t)ctx->g.sz * sizeof(double);
+    double* a = ctx->U[ctx->cur];
+    double* b = ctx->U[1 - ctx->cur];
+    for (int f = 0; f < 8; f++) {
+        double* fa = a + (size_t)f * ctx->ncell;
+        double* fb = b + (size_t)f * ctx->ncell;
+        CK(cudaMemcpyAsync(fb, fa, plane, cudaMemcpyDeviceToDevice, ctx->stream));
+        const size_t last = (size_t)(ctx->g.nz - 1) * ctx->g.sz;
+        CK(cudaMemcpyAsync(fb + last, fa + last, plane, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ctx->ghosts_synced = true;
+    return MHD_OK;
+}
+
+int ensure_parity_buffers(mhd_ctx* ctx) {
+    int rc = alloc_block(ctx, &ctx->Fb, 8);
+    if (rc) return rc;
+    return alloc_block(ctx, &ctx->Sb, 4);
+}
+
+int fused_step(mhd_ctx* ctx, double dt) {
+    int rc = ensure_u1(ctx);
+    if (rc) return rc;
+    if (ctx->sw & kSwShr) {
+        rc = alloc_block(ctx, &ctx->Fb, 8);
+        if (rc) return rc;
+    }
+    rc = sync_zghosts(ctx);
+    if (rc) return rc;
+    const double gam[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
+    const double zet[3] = {ctx->k.ZETA1, ctx->k.ZETA2, 0.0};
+    for (int s = 0; s < 3; s++) {
+        FusedArgs a{};
+        a.g = ctx->g;
+        a.c = ctx->c;
+        a.k = ctx->coef;
+        a.U = fields_of(ctx, ctx->U[ctx->cur]);
+        a.Uo = fields_of(ctx, ctx->U[1 - ctx->cur]);
+        a.Z = fields_of(ctx, ctx->Zb);
+        a.FT = ctx->Fb ? ctx->Fb + (size_t)F_FT * ctx->ncell : nullptr;
+        a.gdt = gam[s] * dt;
+        a.zdt = zet[s] * dt;
+        a.substage = s;
+        cudaEvent_t* ev = nullptr;
+        if (ctx->profiling) {
+            if (ctx->prof_used + 2 > ctx->prof_events.size()) {
+                for (int j = 0; j < 64; j++) {
+                    cudaEvent_t e0;
+                    CK(cudaEventCreate(&e0));
+                    ctx->prof_events.push_back(e0);
+                }
+            }
+            ev = &ctx->prof_events[ctx->prof_used];
+            ctx->prof_used += 2;
+            CK(cudaEventRecord(ev[0], ctx->stream));
+        }
+        int e = fused_substage(ctx->sw, a, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "fused substage launch");
+        if (ev) CK(cudaEventRecord(ev[1], ctx->stream));
+        e = fused_bcon_ghost(ctx->sw, ctx->g, ctx->c, a.Uo, ctx->timt, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "BCON launch");
+        ctx->cur = 1 - ctx->cur;
+    }
+    return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mhd_status_string(int s) {
+    switch (s) {
+        case MHD_OK: return "ok";
+        case MHD_ERR_INVALID: return "invalid argument";
+        case MHD_ERR_UNSUPPORTED: return "unsupported configuration";
+        case MHD_ERR_CUDA: return "CUDA error";
+        case MHD_ERR_NUMERIC: return "non-finite or non-positive state";
+        case MHD_ERR_DT_TOO_SMALL: return "DT too small";
+        case MHD_ERR_NOMEM: return "out of device memory";
+        case MHD_ERR_TIMEOUT: return "device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+const char* mhd_last_error(const mhd_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
+    if (!out) return MHD_ERR_INVALID;
+    *out = nullptr;
+    std::string why;
+    int rc = validate(params, why);
+    if (rc) {
+        fprintf(stderr, "mhd_create: %s\n", why.c_str());
+        return rc;
+    }
+    mhd_ctx* ctx = new mhd_ctx();
+    ctx->prm = *params;
+    const mhd_params& p = ctx->prm;
+    compute_constants(p, ctx->k);
+    ctx->sw = p.switches & (MHD_SW_LROT | MHD_SW_LMAG | MHD_SW_LSHR);
+    ctx->nf = (ctx->sw & MHD_SW_LMAG) ? 8 : 5;
+    ctx->g.nx = p.nPx + 2;
+    ctx->g.ny = p.nPy + 2;
+    ctx->g.nz = p.nPz + 2;
+    ctx->g.nPz = p.nPz;
+    ctx->g.sy = ctx->g.nx;
+    ctx->g.sz = (long long)ctx->g.nx * ctx->g.ny;
+    ctx->ncell = (size_t)ctx->g.sz * ctx->g.nz;
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            fprintf(stderr, "mhd_create: %s\n", cudaGetErrorString(e));
+            delete ctx;
+            return MHD_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    // metric arrays and the premultiplied coefficients of the fused path
+    const int nx = ctx->g.nx, ny = ctx->g.ny, nz = ctx->g.nz;
+    std::vector<double> h;
+    auto put = [&](const double* a, int n) { h.insert(h.end(), a, a + n); };
+    put(p.dxxdx, nx); put(p.d2xxdx2, nx); put(p.DDX, nx);
+    put(p.dyydy, ny); put(p.d2yydy2, ny); put(p.DDY, ny);
+    put(p.dzzdz, nz); put(p.d2zzdz2, nz); put(p.DDZ, nz);
+    put(p.RKAPA, nz); put(p.DKAPA, nz);
+    const double hs[3] = {ctx->k.hx, ctx->k.hy, ctx->k.hz};
+    const double h2s[3] = {ctx->k.h2x, ctx->k.h2y, ctx->k.h2z};
+    const double* d1s[3] = {p.dxxdx, p.dyydy, p.dzzdz};
+    const double* d2s[3] = {p.d2xxdx2, p.d2yydy2, p.d2zzdz2};
+    const int ns[3] = {nx, ny, nz};
+    for (int ax = 0; ax < 3; ax++) {
+        for (int i = 0; i < ns[ax]; i++) h.push_back(d1s[ax][i] * hs[ax]);
+        for (int i = 0; i < ns[ax]; i++) h.push_back(d2s[ax][i] * hs[ax]);
+        for (int i = 0; i < ns[ax]; i++) h.push_back(d1s[ax][i] * d1s[ax][i] * h2s[ax]);
+    }
+    if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        mhd_destroy(ctx);
+        return MHD_ERR_NOMEM;
+    }
+    ctx->bytes += h.size() * sizeof(double);
+    const double* m = ctx->d_metric;
+    Consts& c = ctx->c;
+    c.dxxdx = m; c.d2xxdx2 = m + nx; c.DDX = m + 2 * nx; m += 3 * nx;
+    c.dyydy = m; c.d2yydy2 = m + ny; c.DDY = m + 2 * ny; m += 3 * ny;
+    c.dzzdz = m; c.d2zzdz2 = m + nz; c.DDZ = m + 2 * nz; c.RKAPA = m + 3 * nz; c.DKAPA = m + 4 * nz; m += 5 * nz;
+    ctx->coef.cx1 = m; ctx->coef.cx2a = m + nx; ctx->coef.cx2b = m + 2 * nx; m += 3 * nx;
+    ctx->coef.cy1 = m; ctx->coef.cy2a = m + ny; ctx->coef.cy2b = m + 2 * ny; m += 3 * ny;
+    ctx->coef.cz1 = m; ctx->coef.cz2a = m + nz; ctx->coef.cz2b = m + 2 * nz;
+    c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
+    c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;
+    c.GRAV = p.GRAV; c.THETA = p.THETA; c.RE = p.RE; c.REPR = ctx->k.REPR; c.ORE = ctx->k.ORE;
+    c.OCV = ctx->k.OCV; c.CV = ctx->k.CV; c.GAMMA = p.GAMMA; c.OMX = ctx->k.OMX; c.OMZ = ctx->k.OMZ;
+    c.RM = p.RM; c.ORM = ctx->k.ORM; c.OBETA = ctx->k.OBETA; c.TB = p.TB; c.TP = p.TP; c.SFF = p.SFF;
+    c.izCon = p.izCon; c.iTCon = p.iTCon; c.iBCon = p.iBCon;
+
+    ctx->red_blocks = 152 * 8;
+    int arc = alloc_block(ctx, &ctx->U[0], 8);
+    if (!arc) arc = alloc_block(ctx, &ctx->Zb, 8);
+    if (!arc && cudaMalloc(&ctx->red, sizeof(double) * 8 * (size_t)ctx->red_blocks) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    if (!arc && cudaMalloc(&ctx->d_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    if (!arc && cudaMallocHost(&ctx->h_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    if (arc) {
+        cudaGetLastError();
+        fprintf(stderr, "mhd_create: %s\n", ctx->err.empty() ? "allocation failed" : ctx->err.c_str());
+        mhd_destroy(ctx);
+        return MHD_ERR_NOMEM;
+    }
+    ctx->bytes += sizeof(double) * (8 * (size_t)ctx->red_blocks + 8);
+    ctx->timt = 0.0;
+    ctx->nit = 0;
+    *out = ctx;
+    return MHD_OK;
+}
+
+int mhd_destroy(mhd_ctx* ctx) {
+    if (!ctx) return MHD_ERR_INVALID;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->d_metric);
+    cudaFree(ctx->U[0]);
+    cudaFree(ctx->U[1]);
+    cudaFree(ctx->Zb);
+    cudaFree(ctx->Fb);
+    cudaFree(ctx->Sb);
+    cudaFree(ctx->red);
+    cudaFree(ctx->d_out);
+    if (ctx->h_out) cudaFreeHost(ctx->h_out);
+    if (ctx->t0) cudaEventDestroy(ctx->t0);
+    if (ctx->t1) cudaEventDestroy(ctx->t1);
+    for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MHD_OK;
+}
+
+int mhd_get_constants(const mhd_ctx* ctx, mhd_constants* out) {
+    if (!ctx || !out) return MHD_ERR_INVALID;
+    *out = ctx->k;
+    return MHD_OK;
+}
+
+int mhd_compute_constants(const mhd_params* params, mhd_constants* out) {
+    if (!params || !out) return MHD_ERR_INVALID;
+    compute_constants(*params, *out);
+    return MHD_OK;
+}
+
+int mhd_device_bytes(const mhd_ctx* ctx, size_t* out) {
+    if (!ctx || !out) return MHD_ERR_INVALID;
+    *out = ctx->bytes;
+    return MHD_OK;
+}
+
+static double* field_ptr(mhd_ctx* ctx, int field, bool for_write, int* rc) {
+    *rc = MHD_OK;
+    if (field < 0 || field >= MHD_NFIELDS) {
+        *rc = fail(ctx, MHD_ERR_INVALID, "field id out of range");
+        return nullptr;
+    }
+    if (field < 8) {
+        if (for_write) ctx->ghosts_synced = false;
+        return ctx->U[ctx->cur] + (size_t)field * ctx->ncell;
+    }
+    if (field < 16) {
+        *rc = alloc_block(ctx, &ctx->Fb, 8);
+        return *rc ? nullptr : ctx->Fb + (size_t)(field - 8) * ctx->ncell;
+    }
+    return ctx->Zb + (size_t)(field - 16) * ctx->ncell;
+}
+
+int mhd_upload(mhd_ctx* ctx, int field, const double* host) {
+    if (!ctx || !host) return MHD_ERR_INVALID;
+    int rc;
+    double* d = field_ptr(ctx, field, true, &rc);
+    if (!d) return rc;
+    CK(cudaMemcpyAsync(d, host, field_bytes(ctx), cudaMemcpyHostToDevice, ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_download(mhd_ctx* ctx, int field, double* host) {
+    if (!ctx || !host) return MHD_ERR_INVALID;
+    int rc;
+    double* d = field_ptr(ctx, field, false, &rc);
+    if (!d) return rc;
+    CK(cudaMemcpyAsync(host, d, field_bytes(ctx), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_upload_state(mhd_ctx* ctx, const double* host) {
+    if (!ctx || !host) return MHD_ERR_INVALID;
+    ctx->ghosts_synced = false;
+    CK(cudaMemcpyAsync(ctx->U[ctx->cur], host, field_bytes(ctx) * ctx->nf, cudaMemcpyHostToDevice, ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_download_state(mhd_ctx* ctx, double* host) {
+    if (!ctx || !host) return MHD_ERR_INVALID;
+    CK(cudaMemcpyAsync(host, ctx->U[ctx->cur], field_bytes(ctx) * ctx->nf, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_set_time(mhd_ctx* ctx, double timt, long long nit) {
+    if (!ctx) return MHD_ERR_INVALID;
+    ctx->timt = timt;
+    ctx->nit = nit;
+    return MHD_OK;
+}
+
+int mhd_fluxes(mhd_ctx* ctx) {
+    if (!ctx) return MHD_ERR_INVALID;
+    int rc = ensure_parity_buffers(ctx);
+    if (rc) return rc;
+    double* S = ctx->Sb;
+    ctx->ghosts_synced = false;  // 1/rho is written into RO over every cell, wall ghost planes included
+    const int e = parity_fluxes(ctx->sw, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), fields_of(ctx, ctx->Fb), S,
+                                S + ctx->ncell, S + 2 * ctx->ncell, S + 3 * ctx->ncell, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "fluxes launch");
+    return MHD_OK;
+}
+
+static int rk(mhd_ctx* ctx, int kind, double coef) {
+    if (!ctx) return MHD_ERR_INVALID;
+    int rc = alloc_block(ctx, &ctx->Fb, 8);
+    if (rc) return rc;
+    if (kind == 2) ctx->ghosts_synced = false;
+    const int e = parity_rk(kind, ctx->nf, ctx->g, fields_of(ctx, ctx->U[ctx->cur]), fields_of(ctx, ctx->Zb),
+                            fields_of(ctx, ctx->Fb), coef, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "RK launch");
+    return MHD_OK;
+}
+
+int mhd_rk_zeta0(mhd_ctx* ctx) { return rk(ctx, 0, 0.0); }
+int mhd_rk_zeta(mhd_ctx* ctx, double coef) { return rk(ctx, 1, coef); }
+int mhd_rk_gam(mhd_ctx* ctx, double coef) { return rk(ctx, 2, coef); }
+
+int mhd_bcon(mhd_ctx* ctx, double timt) {
+    if (!ctx) return MHD_ERR_INVALID;
+    const int e = parity_bcon(ctx->sw, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), timt, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "BCON launch");
+    return MHD_OK;
+}
+
+int mhd_communicate(mhd_ctx* ctx) {
+    if (!ctx) return MHD_ERR_INVALID;
+    ctx->ghosts_synced = false;
+    const int e = parity_communicate(ctx->nf, ctx->g, fields_of(ctx, ctx->U[ctx->cur]), ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "communicate launch");
+    return MHD_OK;
+}
+
+int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach) {
+    if (!ctx) return MHD_ERR_INVALID;
+    const bool mag = (ctx->sw & kSwMag) != 0;
+    int e = parity_cfl(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks, ctx->d_out,
+                       ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "CFL launch");
+    CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double* o = ctx->h_out;
+    auto mn = [](double a, double b) { return (b < a) ? b : a; };
+    // 3dmhdsub.h:44,102-104
+    const double d = mag ? ctx->prm.SFF * mn(mn(o[1], o[2]), mn(o[3], o[4])) : ctx->prm.SFF * mn(mn(o[1], o[2]), o[3]);
+    ctx->last_umach = std::sqrt(o[0]);
+    if (umach) *umach = ctx->last_umach;
+    if (dt) *dt = d;
+    if (!(d == d) || !(o[0] == o[0])) return fail(ctx, MHD_ERR_NUMERIC, "non-finite CFL estimate");
+    return MHD_OK;
+}
+
+static int parity_step(mhd_ctx* ctx, double dt) {
+    const double g[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
+    const double zt[2] = {ctx->k.ZETA1, ctx->k.ZETA2};
+    int rc;
+    for (int s = 0; s < 3; s++) {
+        rc = s == 0 ? mhd_rk_zeta0(ctx) : mhd_rk_zeta(ctx, zt[s - 1] * dt);
+        if (rc) return rc;
+        if ((rc = mhd_fluxes(ctx))) return rc;
+        if ((rc = mhd_rk_gam(ctx, g[s] * dt))) return rc;
+        if ((rc = mhd_bcon(ctx, ctx->timt))) return rc;
+        if ((rc = mhd_communicate(ctx))) return rc;
+    }
+    return MHD_OK;
+}
+
+int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out) {
+    if (!ctx) return MHD_ERR_INVALID;
+    int rc;
+    if (!(dt > 0.0)) {
+        rc = mhd_cfl_dt(ctx, &dt, nullptr);
+        if (rc) return rc;
+        if (dt < 1.0e-8f) return fail(ctx, MHD_ERR_DT_TOO_SMALL, "DT too small, halt (3dmhd.cpp:292-331)");
+    }
+    rc = ctx->prm.path == MHD_PATH_PARITY ? parity_step(ctx, dt) : fused_step(ctx, dt);
+    if (rc) return rc;
+    // 3dmhdsub.h:150-152 (TIMI + TIMC accumulates the same way)
+    ctx->nit += 1;
+    ctx->timt += dt;
+    ctx->last_dt = dt;
+    if (out) {
+        memset(out, 0, sizeof(*out));
+        out->dt = dt;
+        out->umach = ctx->last_umach;
+        out->timt = ctx->timt;
+        out->nit = ctx->nit;
+    }
+    return MHD_OK;
+}
+
+int mhd_steps(mhd_ctx* ctx, int n, double dt) {
+    if (!ctx || n < 0 || !(dt > 0.0)) return MHD_ERR_INVALID;
+    for (int s = 0; s < n; s++) {
+        int rc = mhd_step(ctx, dt, nullptr);
+        if (rc) return rc;
+    }
+    return MHD_OK;
+}
+
+int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out) {
+    if (!ctx || !out) return MHD_ERR_INVALID;
+    const bool mag = (ctx->sw & kSwMag) != 0;
+    int e = diag_reduce(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks, ctx->d_out,
+                        ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "diagnostics launch");
+    CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(double) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    memset(out, 0, sizeof(*out));
+    out->total_mass = ctx->h_out[0];
+    out->total_energy = ctx->h_out[1];
+    out->max_divb = ctx->h_out[2];
+    out->flags = (int)ctx->h_out[3];
+    out->dt = ctx->last_dt;
+    out->umach = ctx->last_umach;
+    out->timt = ctx->timt;
+    out->nit = ctx->nit;
+    return out->flags ? fail(ctx, MHD_ERR_NUMERIC, "state has non-finite or non-positive values") : MHD_OK;
+}
+
+int mhd_sync(mhd_ctx* ctx) {
+    if (!ctx) return MHD_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_set_device(int device) {
+    return cudaSetDevice(device) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA;
+}
+
+int mhd_timer_start(mhd_ctx* ctx) {
+    if (!ctx) return MHD_ERR_INVALID;
+    if (!ctx->t0) CK(cudaEventCreate(&ctx->t0));
+    if (!ctx->t1) CK(cudaEventCreate(&ctx->t1));
+    CK(cudaEventRecord(ctx->t0, ctx->stream));
+    return MHD_OK;
+}
+
+int mhd_timer_stop(mhd_ctx* ctx, double* ms) {
+    if (!ctx || !ms || !ctx->t0) return MHD_ERR_INVALID;
+    CK(cudaEventRecord(ctx->t1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->t1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
+    *ms = (double)f;
+    return MHD_OK;
+}
+
+int mhd_profile(mhd_ctx* ctx, int enable) {
+    if (!ctx) return MHD_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->profiling = enable != 0;
+    ctx->prof_used = 0;
+    return MHD_OK;
+}
+
+int mhd_profile_read(mhd_ctx* ctx, double* substage_ms, long long* launches) {
+    if (!ctx) return MHD_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    double tot = 0.0;
+    for (size_t j = 0; j + 1 < ctx->prof_used; j += 2) {
+        float f = 0.f;
+        CK(cudaEventElapsedTime(&f, ctx->prof_events[j], ctx->prof_events[j + 1]));
+        tot += f;
+    }
+    if (substage_ms) *substage_ms = tot;
+    if (launches) *launches = (long long)(ctx->prof_used / 2);
+    return MHD_OK;
+}
+
+int mhd_fp64_peak(double* tflops) {
+    if (!tflops) return MHD_ERR_INVALID;
+    return fp64_peak(tflops) == 0 ? MHD_OK : MHD_ERR_CUDA;
+}
+
+int mhd_host_alloc(size_t bytes, void** out) {
+    if (!out) return MHD_ERR_INVALID;
+    return cudaMallocHost(out, bytes) == cudaSuccess ? MHD_OK : MHD_ERR_NOMEM;
+}
+
+int mhd_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA; }
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// mhd_common.cuh -- device-side definitions shared by the 3dmhd kernels.
+//
+// Layout of every field: double (or float) [nz][ny][nx], x fastest, one ghost
+// cell per side, exactly the reference's `data` type (3dmhddata.h:8) on one
+// global domain.  Strides: sy = nx, sz = nx*ny (elements).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mhd {
+
+// Compile-time physics switches, the reference's 3dmhdparam.h:8-17 and
+// :86-107 macros as template parameters.  Horizontal boundaries are periodic
+// only (fluxes() exits otherwise, 3dmhdsub.h:204-209); lPot is never read by
+// the reference; lRem is out of scope.
+template <bool MAG, bool ROT, bool SHR>
+struct Switches {
+    static constexpr bool lMag = MAG;
+    static constexpr bool lRot = ROT;
+    static constexpr bool lShr = SHR;
+    static constexpr bool lPot = false;
+    static constexpr bool lRem = false;
+    static constexpr int ixCon = 0;
+    static constexpr int iyCon = 0;
+};
+
+// field slots of the state (dump record order, 3dmhdio.h:23-33)
+enum StateSlot { S_RU = 0, S_RV, S_RW, S_TT, S_RO, S_BX, S_BY, S_BZ };
+// field slots of the right-hand sides
+enum FluxSlot { F_FU = 0, F_FV, F_FW, F_FR, F_FT, F_WW1, F_WW2, F_WW3 };
+
+struct Grid {
+    int nx, ny, nz;  // full sizes, ghosts included
+    int nPz;
+    long long sy, sz;
+};
+
+// Scalars of set()/main() (3dmhd.cpp:144-145,354-369,401-459) and device
+// pointers to the 1-D metric arrays (3dmhddata.h:21-23).
+struct Consts {
+    double C13, C23, C43;
+    double hx, h2x, hy, h2y, hz, h2z;
+    double GRAV, THETA, RE, REPR, ORE, OCV, CV, GAMMA, OMX, OMZ, RM, ORM, OBETA, TB, TP, SFF;
+    int izCon, iTCon, iBCon, pad_;
+    const double *dxxdx, *d2xxdx2, *DDX;
+    const double *dyydy, *d2yydy2, *DDY;
+    const double *dzzdz, *d2zzdz2, *DDZ;
+    const double *RKAPA, *DKAPA;
+};
+
+struct Fields8 {
+    double* p[8];
+};
+
+// Metric coefficients premultiplied for the fused kernels:
+//   c1 = duudu*hu, c2a = d2uudu2*hu, c2b = duudu^2*h2u   per axis.
+struct Coefs {
+    const double *cx1, *cx2a, *cx2b;
+    const double *cy1, *cy2a, *cy2b;
+    const double *cz1, *cz2a, *cz2b;
+};
+
+// ---- launchers implemented in the .cu files ----------------------------
+// Parity path (compiled with -fmad=false, bit-exact with the reference).
+int parity_fluxes(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* P, double* UU,
+                  double* VV, double* WW, cudaStream_t st);
+int parity_rk(int kind, int nf, const Grid& g, Fields8 U, Fields8 Z, Fields8 F, double coef, cudaStream_t st);
+int parity_bcon(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
+int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st);
+// CFL partial minima/maxima; out[0..4] = UMACH^2-candidate max, w0..w3 minima.
+int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+               double* out5, cudaStream_t st);
+// Conserved totals and max |div B|; out[0..3] = mass, energy, max divB, flags.
+int diag_reduce(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks, double* out4,
+                cudaStream_t st);
+
+// Measured FP64 FMA throughput of the current device (TFLOP/s, 2 flops per FMA).
+int fp64_peak(double* tflops);
+
+// Fused FP64 path.
+struct FusedArgs {
+    Grid g;
+    Consts c;
+    Coefs k;
+    Fields8 U;     // state read (with ghosts)
+    Fields8 Uo;    // state written (interior + x/y ghost images)
+    Fields8 Z;     // RK register (read when substage > 0, written when substage < 2)
+    double* FT;    // persistent temperature right-hand side (lShr only)
+    double gdt;    // GAM_k * dt
+    double zdt;    // ZETA_k * dt
+    int substage;  // 0, 1, 2
+};
+int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st);
+int fused_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
+
+constexpr unsigned kSwRot = 0x1u, kSwMag = 0x2u, kSwShr = 0x10u;
+
+}  // namespace mhd
+
+// Dispatch a runtime switch word to Switches<MAG,ROT,SHR> template instances.
+#define MHD_DISPATCH_SW(sw, FN, ...)                                                  \
+    do {                                                                              \
+        const bool m_ = ((sw) & ::mhd::kSwMag) != 0;                                  \
+        const bool r_ = ((sw) & ::mhd::kSwRot) != 0;                                  \
+        const bool s_ = ((sw) & ::mhd::kSwShr) != 0;                                  \
+        if (m_ && r_ && s_) FN<::mhd::Switches<true, true, true>>(__VA_ARGS__);       \
+        else if (m_ && r_) FN<::mhd::Switches<true, true, false>>(__VA_ARGS__);       \
+        else if (m_ && s_) FN<::mhd::Switches<true, false, true>>(__VA_ARGS__);       \
+        else if (m_) FN<::mhd::Switches<true, false, false>>(__VA_ARGS__);            \
+        else if (r_ && s_) FN<::mhd::Switches<false, true, true>>(__VA_ARGS__);       \
+        else if (r_) FN<::mhd::Switches<false, true, false>>(__VA_ARGS__);            \
+        else if (s_) FN<::mhd::Switches<false, false, true>>(__VA_ARGS__);            \
+        else FN<::mhd::Switches<false, false, false>>(__VA_ARGS__);                   \
+    } while (0)

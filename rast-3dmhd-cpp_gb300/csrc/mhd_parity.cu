@@ -1,0 +1,576 @@
+// mhd_parity.cu -- the unfused "parity" kernels.  Built with -fmad=false.
+//
+// These reproduce the reference CPU code bit for bit: every right-hand-side
+// term is evaluated with the reference's association and accumulated into
+// its target in the reference's sweep order (3dmhdsub.h:194-696), so the
+// per-cell result of this pointwise replay equals the result of the
+// reference's ~150 whole-array sweeps.  Intermediates the reference keeps in
+// scratch arrays over extended ranges (the derivatives it later
+// differentiates again) are recomputed at the neighbouring node from the
+// same formula, which gives the same bits.
+//
+// Operator conventions (3dmhdutils.h:126-239):
+//   D1_u F = ((F[u+1]-F[u-1]) * duudu[u]) * hu
+//   D2_u F = ((F[u+1]-F[u-1]) * d2uudu2[u]) * hu + (((F[u+1]-2F)+F[u-1]) * duudu^2) * h2u
+//   D1_u(F G) = ((F[u+1]G[u+1] - F[u-1]G[u-1]) * duudu[u]) * hu
+// the scale factor is applied last; a scale of 1 is the identity and -1 a
+// negation.
+#include "mhd_common.cuh"
+
+namespace mhd {
+namespace {
+
+struct Ix {
+    long long i, sy, sz;
+    int x, y, z;
+};
+
+__device__ __forceinline__ double d1x(const double* F, long long i, int x, const Consts& c) {
+    return ((F[i + 1] - F[i - 1]) * c.dxxdx[x]) * c.hx;
+}
+__device__ __forceinline__ double d1y(const double* F, long long i, long long sy, int y, const Consts& c) {
+    return ((F[i + sy] - F[i - sy]) * c.dyydy[y]) * c.hy;
+}
+__device__ __forceinline__ double d1z(const double* F, long long i, long long sz, int z, const Consts& c) {
+    return ((F[i + sz] - F[i - sz]) * c.dzzdz[z]) * c.hz;
+}
+__device__ __forceinline__ double d2x(const double* F, long long i, int x, const Consts& c) {
+    const double du = c.dxxdx[x];
+    return ((F[i + 1] - F[i - 1]) * c.d2xxdx2[x]) * c.hx + (((F[i + 1] - 2 * F[i]) + F[i - 1]) * (du * du)) * c.h2x;
+}
+__device__ __forceinline__ double d2y(const double* F, long long i, long long sy, int y, const Consts& c) {
+    const double du = c.dyydy[y];
+    return ((F[i + sy] - F[i - sy]) * c.d2yydy2[y]) * c.hy + (((F[i + sy] - 2 * F[i]) + F[i - sy]) * (du * du)) * c.h2y;
+}
+__device__ __forceinline__ double d2z(const double* F, long long i, long long sz, int z, const Consts& c) {
+    const double du = c.dzzdz[z];
+    return ((F[i + sz] - F[i - sz]) * c.d2zzdz2[z]) * c.hz + (((F[i + sz] - 2 * F[i]) + F[i - sz]) * (du * du)) * c.h2z;
+}
+__device__ __forceinline__ double mdx(const double* F, const double* G, long long i, int x, const Consts& c) {
+    return ((F[i + 1] * G[i + 1] - F[i - 1] * G[i - 1]) * c.dxxdx[x]) * c.hx;
+}
+__device__ __forceinline__ double mdy(const double* F, const double* G, long long i, long long sy, int y,
+                                      const Consts& c) {
+    return ((F[i + sy] * G[i + sy] - F[i - sy] * G[i - sy]) * c.dyydy[y]) * c.hy;
+}
+__device__ __forceinline__ double mdz(const double* F, const double* G, long long i, long long sz, int z,
+                                      const Consts& c) {
+    return ((F[i + sz] * G[i + sz] - F[i - sz] * G[i - sz]) * c.dzzdz[z]) * c.hz;
+}
+
+// Pressure, gravity, 1/rho in place and the velocities over the extended
+// range (3dmhdsub.h:266-268,274-276).
+__global__ void k_prep(Grid g, Consts c, Fields8 U, double* FW, double* P, double* UU, double* VV, double* WW) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx);
+        const int y = (int)((i / g.nx) % g.ny);
+        const int z = (int)(i / g.sz);
+        const double ro = U.p[S_RO][i];
+        if (x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1) FW[i] = ro * c.GRAV;
+        P[i] = ro * U.p[S_TT][i];
+        const double ri = 1.0 / ro;
+        U.p[S_RO][i] = ri;
+        UU[i] = U.p[S_RU][i] * ri;
+        VV[i] = U.p[S_RV][i] * ri;
+        WW[i] = U.p[S_RW][i] * ri;
+    }
+}
+
+template <class SW>
+__global__ void k_flux(Grid g, Consts c, Fields8 U, Fields8 F, const double* __restrict__ P,
+                       const double* __restrict__ UU, const double* __restrict__ VV, const double* __restrict__ WW) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
+    const long long ncell = (long long)nPx * nPy * nPz;
+    const long long sy = g.sy, sz = g.sz;
+    const int zl = 1, zr = g.nz - 1;
+    const double *RU = U.p[S_RU], *RV = U.p[S_RV], *RW = U.p[S_RW], *TT = U.p[S_TT], *RI = U.p[S_RO];
+    const double *BX = U.p[S_BX], *BY = U.p[S_BY], *BZ = U.p[S_BZ];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t % nPx);
+        const int y = 1 + (int)((t / nPx) % nPy);
+        const int z = 1 + (int)(t / ((long long)nPx * nPy));
+        const long long i = z * sz + y * sy + x;
+
+        // continuity, 3dmhdsub.h:204-227
+        double fr = -d1x(RU, i, x, c);
+        fr -= d1y(RV, i, sy, y, c);
+        double w1 = d1z(RW, i, sz, z, c);
+        if (z == zl) w1 = (4.0f * RW[i + sz] - RW[i + 2 * sz]) * (c.hz * c.dzzdz[zl]);
+        if (z == zr - 1) w1 = (RW[i - 2 * sz] - 4.0f * RW[i - sz]) * (c.hz * c.dzzdz[zr - 1]);
+        fr -= w1;
+
+        // pressure and gravity, 3dmhdsub.h:266-272 (F.FW holds RO*GRAV from k_prep)
+        double fw = F.p[F_FW][i];
+        fw -= d1z(P, i, sz, z, c);
+        double fv = -d1y(P, i, sy, y, c);
+        double fu = -d1x(P, i, x, c);
+
+        // momentum advection, 3dmhdsub.h:279-289
+        fu -= mdx(RU, UU, i, x, c);
+        fu -= mdy(RU, VV, i, sy, y, c);
+        fu -= mdz(RU, WW, i, sz, z, c);
+        fv -= mdx(RV, UU, i, x, c);
+        fv -= mdy(RV, VV, i, sy, y, c);
+        fv -= mdz(RV, WW, i, sz, z, c);
+        fw -= mdx(RW, UU, i, x, c);
+        fw -= mdy(RW, VV, i, sy, y, c);
+        fw -= mdz(RW, WW, i, sz, z, c);
+
+        const double ri = RI[i], tt = TT[i];
+        // temperature advection, 3dmhdsub.h:293-296.  With lShr the reference
+        // never re-initialises FT, so it keeps accumulating across calls.
+        double ft;
+        if constexpr (!SW::lShr) {
+            ft = -(d1x(TT, i, x, c) * UU[i]);
+            ft -= d1y(TT, i, sy, y, c) * VV[i];
+            ft -= d1z(TT, i, sz, z, c) * WW[i];
+        } else {
+            ft = F.p[F_FT][i];
+        }
+        // conduction, 3dmhdsub.h:315-319
+        double tmp = c.OCV / c.REPR;
+        ft += ((d2x(TT, i, x, c) * ri) * c.RKAPA[z]) * tmp;
+        ft += ((d2y(TT, i, sy, y, c) * ri) * c.RKAPA[z]) * tmp;
+        ft += ((d2z(TT, i, sz, z, c) * ri) * c.RKAPA[z]) * tmp;
+        ft += ((d1z(TT, i, sz, z, c) * ri) * c.DKAPA[z]) * tmp;
+
+        // viscous Laplacians, 3dmhdsub.h:462-472
+        fu += d2x(UU, i, x, c) * (c.ORE * c.C43);
+        fu += d2y(UU, i, sy, y, c) * c.ORE;
+        fu += d2z(UU, i, sz, z, c) * c.ORE;
+        fv += d2x(VV, i, x, c) * c.ORE;
+        fv += d2y(VV, i, sy, y, c) * (c.ORE * c.C43);
+        fv += d2z(VV, i, sz, z, c) * c.ORE;
+        fw += d2x(WW, i, x, c) * c.ORE;
+        fw += d2y(WW, i, sy, y, c) * c.ORE;
+        fw += d2z(WW, i, sz, z, c) * (c.ORE * c.C43);
+
+        // viscous cross terms, heating and pdV work, 3dmhdsub.h:475-538
+        const double c13ore = c.C13 * c.ORE;
+        const double ux = d1x(UU, i, x, c);  // WW1 of do 650
+        const double vx = d1x(VV, i, x, c);  // WW2 of do 670
+        double vy = 0.0;
+        if constexpr (!SW::lShr) {
+            const double wx = d1x(WW, i, x, c);  // do 690
+            tmp = c.OCV * c.ORE;
+            ft += ((ri * ux) * ux) * (tmp * c.C43);
+            ft += ((ri * vx) * vx) * tmp;
+            ft += ((ri * wx) * wx) * tmp;
+            ft -= (ux * tt) * c.OCV;
+        }
+        fu += (((d1x(VV, i + sy, x, c) - d1x(VV, i - sy, x, c)) * c.dyydy[y]) * c.hy) * c13ore;  // do 720
+        fv += (((d1x(UU, i + sy, x, c) - d1x(UU, i - sy, x, c)) * c.dyydy[y]) * c.hy) * c13ore;  // do 730
+        if constexpr (!SW::lShr) {
+            const double uy = d1y(UU, i, sy, y, c);  // do 740
+            tmp = c.OCV * c.ORE;
+            ft += ((ri * uy) * uy) * tmp;
+            ft += ((ri * uy) * vx) * (tmp * 2);
+            vy = d1y(VV, i, sy, y, c);  // do 755
+            tmp = c.C43 * c.OCV * c.ORE;
+            ft += ((ri * vy) * vy) * tmp;
+            ft -= (vy * tt) * c.OCV;
+        }
+        const double wz = d1z(WW, i, sz, z, c);  // do 790
+        if constexpr (!SW::lShr) {
+            tmp = c.C43 * c.OCV * c.ORE;
+            ft += ((ri * wz) * wz) * tmp;
+            ft += ((ri * ux) * wz) * (-tmp);
+            ft += ((ri * ux) * vy) * (-tmp);
+            ft += ((ri * vy) * wz) * (-tmp);
+            ft -= (wz * tt) * c.OCV;
+        }
+        fu += (((d1z(WW, i + 1, sz, z, c) - d1z(WW, i - 1, sz, z, c)) * c.dxxdx[x]) * c.hx) * c13ore;   // do 840
+        fv += (((d1z(WW, i + sy, sz, z, c) - d1z(WW, i - sy, sz, z, c)) * c.dyydy[y]) * c.hy) * c13ore; // do 850
+        const double uz = d1z(UU, i, sz, z, c);  // do 860
+        const double vz = d1z(VV, i, sz, z, c);  // do 880
+        if constexpr (!SW::lShr) {
+            const double wy = d1y(WW, i, sy, y, c);  // do 900
+            tmp = c.OCV * c.ORE;
+            ft += ((ri * uz) * uz) * tmp;
+            ft += ((ri * vz) * vz) * tmp;
+            ft += ((ri * wy) * wy) * tmp;
+            ft += ((ri * vz) * wy) * (2.0f * tmp);
+        }
+        fw += (((d1z(UU, i + 1, sz, z, c) - d1z(UU, i - 1, sz, z, c)) * c.dxxdx[x]) * c.hx) * c13ore;   // do 920.1
+        fw += (((d1z(VV, i + sy, sz, z, c) - d1z(VV, i - sy, sz, z, c)) * c.dyydy[y]) * c.hy) * c13ore; // do 920.2
+        if constexpr (!SW::lShr) {
+            const double wx = d1x(WW, i, x, c);  // do 930
+            tmp = c.OCV * c.ORE;
+            ft += ((ri * uz) * wx) * (2.0f * tmp);
+        }
+
+        // Coriolis, 3dmhdsub.h:540-545
+        if constexpr (SW::lRot) {
+            fu += RV[i] * c.OMZ;
+            fv -= RU[i] * c.OMZ;
+            fv += RW[i] * c.OMX;
+            fw -= RV[i] * c.OMX;
+        }
+
+        // induction, Lorentz force and Ohmic heating, 3dmhdsub.h:547-695.
+        // sRU..sTT stand for the reference's reuse of RU, RV, RW, TT as scratch.
+        if constexpr (SW::lMag) {
+            const double c1 = c.OBETA * c.ORM * c.OCV;
+            const double c2 = -2.0f * c.OBETA * c.ORM * c.OCV;
+            const double bx = BX[i], by = BY[i], bz = BZ[i];
+            const double u = UU[i], v = VV[i], w = WW[i];
+            double sRU = d1x(UU, i, x, c), sRV = d1x(VV, i, x, c), sRW = d1x(WW, i, x, c), sTT;
+            double ww2 = bx * sRV;
+            ww2 -= by * sRU;
+            double ww3 = bx * sRW;
+            ww3 -= bz * sRU;
+            sRU = d1y(UU, i, sy, y, c);
+            sRV = d1y(VV, i, sy, y, c);
+            sRW = d1y(WW, i, sy, y, c);
+            double ww1 = by * sRU;
+            ww1 -= bx * sRV;
+            ww3 += by * sRW;
+            ww3 -= bz * sRV;
+            sRU = d1z(UU, i, sz, z, c);
+            sRV = d1z(VV, i, sz, z, c);
+            sRW = d1z(WW, i, sz, z, c);
+            if (z == zl) sRW = (4.0f * WW[i + sz] - WW[i + 2 * sz]) * c.hz * c.dzzdz[zl];
+            if (z == zr - 1) sRW = (-4.0f * WW[i - sz] + WW[i - 2 * sz]) * c.hz * c.dzzdz[zr - 1];
+            ww1 += bz * sRU;
+            ww1 -= bx * sRW;
+            ww2 += bz * sRV;
+            ww2 -= by * sRW;
+            sRU = d1x(BX, i, x, c);
+            sRV = d1x(BY, i, x, c);
+            sRW = d1x(BZ, i, x, c);
+            sTT = d1y(BX, i, sy, y, c);
+            fu += (by * sTT) * c.OBETA;
+            fu -= (by * sRV) * c.OBETA;
+            fu -= (bz * sRW) * c.OBETA;
+            fv += (bx * sRV) * c.OBETA;
+            fv -= (bx * sTT) * c.OBETA;
+            fw += (bx * sRW) * c.OBETA;
+            ft += ((ri * sTT) * sTT) * c1;
+            ft += ((ri * sRV) * sRV) * c1;
+            ft += ((ri * sRW) * sRW) * c1;
+            ft += ((ri * sRV) * sTT) * c2;
+            ww1 -= u * sRU;
+            ww1 -= v * sTT;
+            ww2 -= u * sRV;
+            ww3 -= u * sRW;
+            sRU = d2x(BX, i, x, c);
+            sRV = d2x(BY, i, x, c);
+            sTT = d2y(BX, i, sy, y, c);
+            ww1 += sRU * c.ORM;
+            ww1 += sTT * c.ORM;
+            ww2 += sRV * c.ORM;
+            sTT = d2x(BZ, i, x, c);
+            ww3 += sTT * c.ORM;
+            sRU = d1z(BX, i, sz, z, c);
+            sRV = d1y(BY, i, sy, y, c);
+            fu += (bz * sRU) * c.OBETA;
+            fw -= (bx * sRU) * c.OBETA;
+            ft += ((ri * sRU) * sRU) * c1;
+            ft += ((ri * sRU) * sRW) * c2;
+            ww1 -= w * sRU;
+            ww2 -= v * sRV;
+            sRU = d2z(BX, i, sz, z, c);
+            if (z == zl)
+                sRU = (-3.0f * BX[i] + 4.0f * BX[i + sz] - BX[i + 2 * sz]) * c.hz * c.d2zzdz2[zl] +
+                      (2.0f * BX[i] - 5.0f * BX[i + sz] + 4.0f * BX[i + 2 * sz] - BX[i + 3 * sz]) * c.h2z * c.dzzdz[zl] *
+                          c.dzzdz[zl];
+            if (z == zr - 1)
+                sRU = (3.0f * BX[i] - 4.0f * BX[i - sz] + BX[i - 2 * sz]) * c.hz * c.d2zzdz2[zr - 1] +
+                      (2.0f * BX[i] - 5.0f * BX[i - sz] + 4.0f * BX[i - 2 * sz] - BX[i - 3 * sz]) * c.h2z *
+                          c.dzzdz[zr - 1] * c.dzzdz[zr - 1];
+            sRV = d2y(BY, i, sy, y, c);
+            ww1 += sRU * c.ORM;
+            ww2 += sRV * c.ORM;
+            sRV = d1z(BY, i, sz, z, c);
+            sRW = d1y(BZ, i, sy, y, c);
+            sRU = sRV;
+            sRU -= sRW;
+            fv += (bz * sRU) * c.OBETA;
+            fw -= (by * sRU) * c.OBETA;
+            ft += ((ri * sRV) * sRV) * c1;
+            ft += ((ri * sRW) * sRW) * c1;
+            ft += ((ri * sRV) * sRW) * c2;
+            ww2 -= w * sRV;
+            ww3 -= v * sRW;
+            sRV = d2z(BY, i, sz, z, c);
+            if (z == zl)
+                sRV = (-3.0f * BY[i] + 4.0f * BY[i + sz] - BY[i + 2 * sz]) * c.hz * c.d2zzdz2[zl] +
+                      (2.0f * BY[i] - 5.0f * BY[i + sz] + 4.0f * BY[i + 2 * sz] - BY[i + 3 * sz]) * c.h2z * c.dzzdz[zl] *
+                          c.dzzdz[zl];
+            if (z == zr - 1)
+                sRV = (3.0f * BY[i] - 4.0f * BY[i - sz] + BY[i - 2 * sz]) * c.hz * c.d2zzdz2[zr - 1] +
+                      (2.0f * BY[i] - 5.0f * BY[i - sz] + 4.0f * BY[i - 2 * sz] - BY[i - 3 * sz]) * c.h2z *
+                          c.dzzdz[zr - 1] * c.dzzdz[zr - 1];
+            sRW = d2y(BZ, i, sy, y, c);
+            ww2 += sRV * c.ORM;
+            ww3 += sRW * c.ORM;
+            sRW = d1z(BZ, i, sz, z, c);
+            ww3 -= w * sRW;
+            sRW = d2z(BZ, i, sz, z, c);
+            ww3 += sRW * c.ORM;
+            F.p[F_WW1][i] = ww1;
+            F.p[F_WW2][i] = ww2;
+            F.p[F_WW3][i] = ww3;
+        }
+        F.p[F_FU][i] = fu;
+        F.p[F_FV][i] = fv;
+        F.p[F_FW][i] = fw;
+        F.p[F_FR][i] = fr;
+        F.p[F_FT][i] = ft;
+    }
+}
+
+// step_block_ZETA0 / ZETA / GAM over the interior, scale_add = src1 + scale*srcd1
+// (3dmhdsub.h:155-192, 3dmhdutils.h:57-59).  kind 0: Z=U, 1: Z=U+c*F, 2: U=Z+c*F.
+__constant__ int kFluxOfState[8] = {F_FU, F_FV, F_FW, F_FT, F_FR, F_WW1, F_WW2, F_WW3};
+
+__global__ void k_rk(int kind, int nf, Grid g, Fields8 U, Fields8 Z, Fields8 F, double coef) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
+    const long long ncell = (long long)nPx * nPy * nPz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t % nPx);
+        const int y = 1 + (int)((t / nPx) % nPy);
+        const int z = 1 + (int)(t / ((long long)nPx * nPy));
+        const long long i = z * g.sz + y * g.sy + x;
+        for (int f = 0; f < nf; f++) {
+            if (kind == 0) Z.p[f][i] = U.p[f][i];
+            else if (kind == 1) Z.p[f][i] = U.p[f][i] + coef * F.p[kFluxOfState[f]][i];
+            else U.p[f][i] = Z.p[f][i] + coef * F.p[kFluxOfState[f]][i];
+        }
+    }
+}
+
+// BCON, 3dmhdsub.h:720-873.  One thread per (y, x) of the interior does the
+// top wall (z = 1, rank row myPEz == 0 in the reference) and the bottom wall
+// (z = nz-2, myPEz == nPEz-1).
+template <class SW>
+__global__ void k_bcon(Grid g, Consts c, Fields8 U, double timt) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nPx * nPy) return;
+    const int x = 1 + t % nPx, y = 1 + t / nPx;
+    const long long sz = g.sz;
+    double *RU = U.p[S_RU], *RV = U.p[S_RV], *RW = U.p[S_RW], *TT = U.p[S_TT], *RO = U.p[S_RO], *BZ = U.p[S_BZ];
+    const double RRT = 1.0f, RRB = -1.0f, RPP = 0.0f;
+    const int zl = 1, zr = g.nz - 1;
+    // top
+    long long i = zl * sz + y * g.sy + x;
+    if constexpr (SW::lShr) {
+        RU[i] = 0.0f;
+        RV[i] = RRT * cos(RPP * timt) * RO[i];
+    } else {
+        RU[i] = RO[i] * (c.C43 * RU[i + sz] / RO[i + sz] - c.C13 * RU[i + 2 * sz] / RO[i + 2 * sz]);
+        RV[i] = RO[i] * (c.C43 * RV[i + sz] / RO[i + sz] - c.C13 * RV[i + 2 * sz] / RO[i + 2 * sz]);
+    }
+    RW[i] = 0.0f;
+    if (c.iTCon == 1) {
+        const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[zl];
+        TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] - c.C23 * DZ * c.THETA;
+    } else {
+        TT[i] = 1.0f;
+        if (c.iTCon == 4 && x < g.nx / 2) TT[i] = 1.0f - c.TP;
+    }
+    if constexpr (SW::lMag) {
+        if (c.iBCon == 0) BZ[i] = 0.0f;
+    }
+    // bottom
+    i = (zr - 1) * sz + y * g.sy + x;
+    if constexpr (SW::lShr) {
+        RU[i] = 0.0f;
+        RV[i] = RRB * cos(RPP * timt) * RO[i];
+    } else {
+        RU[i] = RO[i] * (c.C43 * RU[i - sz] / RO[i - sz] - c.C13 * RU[i - 2 * sz] / RO[i - 2 * sz]);
+        RV[i] = RO[i] * (c.C43 * RV[i - sz] / RO[i - sz] - c.C13 * RV[i - 2 * sz] / RO[i - 2 * sz]);
+    }
+    RW[i] = 0.0f;
+    if (c.izCon == 0) {
+        TT[i] = c.TB;
+    } else {
+        const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[zr - 1];
+        TT[i] = c.C43 * TT[i - sz] - c.C13 * TT[i - 2 * sz] - c.C23 * DZ * c.THETA / c.RKAPA[zr - 1];
+    }
+    if constexpr (SW::lMag) {
+        if (c.iBCon == 0) BZ[i] = 0.0f;
+    }
+}
+
+// communicate(), 3dmhdmpi.h:11-143, on one domain: each x/y ghost cell of
+// every plane (wall ghost planes included) takes the value of its periodic
+// image V[z][wrap(y)][wrap(x)], wrap(0) = n-2, wrap(n-1) = 1.  Sources are
+// never ghosts, so one pass has no ordering hazard.
+__global__ void k_comm(int nf, Grid g, Fields8 U) {
+    const long long per_plane = 2LL * g.nx + 2LL * (g.ny - 2);
+    const long long n = per_plane * g.nz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(t / per_plane);
+        long long r = t % per_plane;
+        int y, x;
+        if (r < g.nx) {
+            y = 0;
+            x = (int)r;
+        } else if (r < 2LL * g.nx) {
+            y = g.ny - 1;
+            x = (int)(r - g.nx);
+        } else {
+            r -= 2LL * g.nx;
+            y = 1 + (int)(r / 2);
+            x = (r % 2) ? g.nx - 1 : 0;
+        }
+        const int ys = (y == 0) ? g.ny - 2 : (y == g.ny - 1 ? 1 : y);
+        const int xs = (x == 0) ? g.nx - 2 : (x == g.nx - 1 ? 1 : x);
+        const long long d = z * g.sz + y * g.sy + x, s = z * g.sz + ys * g.sy + xs;
+        for (int f = 0; f < nf; f++) U.p[f][d] = U.p[f][s];
+    }
+}
+
+// CFL candidates of step() (3dmhdsub.h:36-106), reduced per block; min/max
+// are exact, so the block order does not change the result.
+template <bool MAG>
+__global__ void k_cfl(Grid g, Consts c, Fields8 U, double* part) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
+    const long long ncell = (long long)nPx * nPy * nPz;
+    const double OGAMMA = 1.0f / c.GAMMA;
+    double um = 0.0f, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t % nPx);
+        const int y = 1 + (int)((t / nPx) % nPy);
+        const int z = 1 + (int)(t / ((long long)nPx * nPy));
+        const long long i = z * g.sz + y * g.sy + x;
+        const double ru = U.p[S_RU][i], rv = U.p[S_RV][i], rw = U.p[S_RW][i], ro = U.p[S_RO][i], tt = U.p[S_TT][i];
+        double UU = (ru * ru + rv * rv + rw * rw) / (ro * ro);
+        const double mc = OGAMMA * UU / tt;
+        um = (um < mc) ? mc : um;
+        if constexpr (MAG) {
+            const double bx = U.p[S_BX][i], by = U.p[S_BY][i], bz = U.p[S_BZ][i];
+            UU += c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro +
+                  2.0f * sqrt(UU * (c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro));
+        } else {
+            UU += c.GAMMA * tt + 2.0f * sqrt(c.GAMMA * UU * tt);
+        }
+        double DD = (c.DDZ[z] < c.DDY[y]) ? c.DDZ[z] : c.DDY[y];
+        if (g.nx > 3) DD = (c.DDX[x] < DD) ? c.DDX[x] : DD;
+        const double a0 = DD / sqrt(UU);
+        const double a1 = 0.5f * DD * DD * c.REPR * c.CV * ro / c.RKAPA[z];
+        const double a2 = 0.375f * DD * DD * c.RE * ro;
+        w0 = (a0 < w0) ? a0 : w0;
+        w1 = (a1 < w1) ? a1 : w1;
+        w2 = (a2 < w2) ? a2 : w2;
+        if constexpr (MAG) {
+            const double a3 = 0.5f * DD * DD * c.RM;
+            w3 = (a3 < w3) ? a3 : w3;
+        }
+    }
+    __shared__ double s[5][256];
+    s[0][threadIdx.x] = um;
+    s[1][threadIdx.x] = w0;
+    s[2][threadIdx.x] = w1;
+    s[3][threadIdx.x] = w2;
+    s[4][threadIdx.x] = w3;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            const double a = s[0][threadIdx.x + h];
+            s[0][threadIdx.x] = (s[0][threadIdx.x] < a) ? a : s[0][threadIdx.x];
+            for (int k = 1; k < 5; k++) {
+                const double b = s[k][threadIdx.x + h];
+                s[k][threadIdx.x] = (b < s[k][threadIdx.x]) ? b : s[k][threadIdx.x];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 5; k++) part[(long long)k * gridDim.x + blockIdx.x] = s[k][0];
+}
+
+__global__ void k_cfl_finish(const double* part, int nb, double* out) {
+    __shared__ double s[5][256];
+    double v[5] = {0.0, 1e99, 1e99, 1e99, 1e99};
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const double a = part[b];
+        v[0] = (v[0] < a) ? a : v[0];
+        for (int k = 1; k < 5; k++) {
+            const double q = part[(long long)k * nb + b];
+            v[k] = (q < v[k]) ? q : v[k];
+        }
+    }
+    for (int k = 0; k < 5; k++) s[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            const double a = s[0][threadIdx.x + h];
+            s[0][threadIdx.x] = (s[0][threadIdx.x] < a) ? a : s[0][threadIdx.x];
+            for (int k = 1; k < 5; k++) {
+                const double b = s[k][threadIdx.x + h];
+                s[k][threadIdx.x] = (b < s[k][threadIdx.x]) ? b : s[k][threadIdx.x];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 5; k++) out[k] = s[k][0];
+}
+
+int grid_for(long long n, int threads, int cap) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+template <class SW>
+void launch_flux(const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* P, double* UU, double* VV, double* WW,
+                 cudaStream_t st) {
+    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
+    k_flux<SW><<<grid_for(ncell, 128, 152 * 64), 128, 0, st>>>(g, c, U, F, P, UU, VV, WW);
+}
+
+template <class SW>
+void launch_bcon(const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st) {
+    const int n = (g.nx - 2) * (g.ny - 2);
+    k_bcon<SW><<<(n + 127) / 128, 128, 0, st>>>(g, c, U, timt);
+}
+
+}  // namespace
+
+int parity_fluxes(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* P, double* UU,
+                  double* VV, double* WW, cudaStream_t st) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    k_prep<<<grid_for(n, 256, 152 * 32), 256, 0, st>>>(g, c, U, F.p[F_FW], P, UU, VV, WW);
+    MHD_DISPATCH_SW(sw, launch_flux, g, c, U, F, P, UU, VV, WW, st);
+    return (int)cudaGetLastError();
+}
+
+int parity_rk(int kind, int nf, const Grid& g, Fields8 U, Fields8 Z, Fields8 F, double coef, cudaStream_t st) {
+    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
+    k_rk<<<grid_for(ncell, 256, 152 * 32), 256, 0, st>>>(kind, nf, g, U, Z, F, coef);
+    return (int)cudaGetLastError();
+}
+
+int parity_bcon(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st) {
+    MHD_DISPATCH_SW(sw, launch_bcon, g, c, U, timt, st);
+    return (int)cudaGetLastError();
+}
+
+int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st) {
+    const long long n = (2LL * g.nx + 2LL * (g.ny - 2)) * g.nz;
+    k_comm<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(nf, g, U);
+    return (int)cudaGetLastError();
+}
+
+int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks, double* out5,
+               cudaStream_t st) {
+    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
+    const int nb = grid_for(ncell, 256, max_blocks);
+    if (mag) k_cfl<true><<<nb, 256, 0, st>>>(g, c, U, partials);
+    else k_cfl<false><<<nb, 256, 0, st>>>(g, c, U, partials);
+    k_cfl_finish<<<1, 256, 0, st>>>(partials, nb, out5);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace mhd

@@ -1,0 +1,171 @@
+"""Host-side mirror of the reference's per-timestep interface over the C ABI.
+
+``Simulation`` exposes the reference's entry points under their own names
+(fluxes, step_block_ZETA0/ZETA/GAM, BCON, communicate, step; 3dmhdsub.h:18-22,
+3dmhdmpi.h:11) so a test or a driver reads like the reference's own code,
+while every call runs on the GPU through libmhd_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .case import Case, STATE_FIELDS, metrics
+
+
+def params_for(case: Case, path: str = "fused", precision: str = "fp64") -> tuple[abi.MhdParams, list]:
+    """mhd_params for a case; returns the struct and the arrays it points to."""
+    m = metrics(case)
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in m.arrays()]
+    p = abi.MhdParams()
+    p.nPx, p.nPy, p.nPz = case.nPx, case.nPy, case.nPz
+    p.switches = (abi.SW_LROT if case.lRot else 0) | (abi.SW_LMAG if case.lMag else 0) | \
+                 (abi.SW_LSHR if case.lShr else 0)
+    p.ixCon = p.iyCon = 0
+    p.izCon, p.iTCon, p.iBCon = case.izCon, case.iTCon, case.iBCon
+    p.precision = abi.PREC_FP64 if precision == "fp64" else abi.PREC_FP32
+    p.path = abi.PATH_FUSED if path == "fused" else abi.PATH_PARITY
+    for k in ("RE", "PR", "THETA", "GRAV", "RY", "ANG", "RM", "BETA", "TP", "GAMMA", "SFF"):
+        setattr(p, k, float(getattr(case, k)))
+    p.TB = case.tb
+    names = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
+    for n, a in zip(names, keep):
+        setattr(p, n, a.ctypes.data_as(C.POINTER(C.c_double)))
+    return p, keep
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Simulation:
+    """One device-resident 3dmhd instance."""
+
+    def __init__(self, case: Case, path: str = "fused", precision: str = "fp64", metric_override: dict | None = None):
+        self.case = case
+        self.L = abi.load()
+        p, keep = params_for(case, path, precision)
+        if metric_override:
+            names = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
+            for j, n in enumerate(names):
+                if n in metric_override:
+                    keep[j] = np.ascontiguousarray(metric_override[n], dtype=np.float64)
+                    setattr(p, n, _dp(keep[j]))
+        ctx = C.c_void_p()
+        st = self.L.mhd_create(C.byref(p), None, C.byref(ctx))
+        if st != abi.MHD_OK:
+            raise abi.MhdError(st, "mhd_create failed")
+        self.ctx = ctx
+        self._keep = keep
+        self.timt = 0.0
+
+    # ---- lifetime ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.L.mhd_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st: int) -> None:
+        abi.check(st, self.ctx)
+
+    def constants(self) -> dict:
+        k = abi.MhdConstants()
+        self._ck(self.L.mhd_get_constants(self.ctx, C.byref(k)))
+        return {n: getattr(k, n) for n, _ in k._fields_}
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        self._ck(self.L.mhd_device_bytes(self.ctx, C.byref(b)))
+        return b.value
+
+    # ---- transfers --------------------------------------------------------
+    def upload(self, field: str, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.shape == self.case.shape
+        self._ck(self.L.mhd_upload(self.ctx, abi.FIELD_IDS[field], _dp(a)))
+        self._ck(self.L.mhd_sync(self.ctx))
+
+    def download(self, field: str) -> np.ndarray:
+        out = np.empty(self.case.shape)
+        self._ck(self.L.mhd_download(self.ctx, abi.FIELD_IDS[field], _dp(out)))
+        return out
+
+    def upload_state(self, state: dict) -> None:
+        for k in STATE_FIELDS[:self.case.nfields]:
+            self.upload(k, state[k])
+
+    def download_state(self) -> dict:
+        return {k: self.download(k) for k in STATE_FIELDS[:self.case.nfields]}
+
+    def set_time(self, timt: float, nit: int = 0) -> None:
+        self.timt = timt
+        self._ck(self.L.mhd_set_time(self.ctx, timt, nit))
+
+    # ---- the reference's entry points ---------------------------------------
+    def fluxes(self) -> None:
+        self._ck(self.L.mhd_fluxes(self.ctx))
+
+    def step_block_ZETA0(self) -> None:
+        self._ck(self.L.mhd_rk_zeta0(self.ctx))
+
+    def step_block_ZETA(self, coef: float) -> None:
+        self._ck(self.L.mhd_rk_zeta(self.ctx, coef))
+
+    def step_block_GAM(self, coef: float) -> None:
+        self._ck(self.L.mhd_rk_gam(self.ctx, coef))
+
+    def BCON(self, timt: float | None = None) -> None:
+        self._ck(self.L.mhd_bcon(self.ctx, self.timt if timt is None else timt))
+
+    def communicate(self) -> None:
+        self._ck(self.L.mhd_communicate(self.ctx))
+
+    def cfl_dt(self) -> tuple[float, float]:
+        dt, um = C.c_double(), C.c_double()
+        self._ck(self.L.mhd_cfl_dt(self.ctx, C.byref(dt), C.byref(um)))
+        return dt.value, um.value
+
+    def step(self, dt: float | None = None) -> dict:
+        """One RK3 step; dt None uses the case's fixed dt, dt <= 0 the CFL step."""
+        d = abi.MhdDiag()
+        self._ck(self.L.mhd_step(self.ctx, self.case.dt if dt is None else dt, C.byref(d)))
+        self.timt = d.timt
+        return d.as_dict()
+
+    def steps(self, n: int, dt: float | None = None) -> None:
+        self._ck(self.L.mhd_steps(self.ctx, n, self.case.dt if dt is None else dt))
+
+    # ---- timing on the context's stream -------------------------------------
+    def timer_start(self) -> None:
+        self._ck(self.L.mhd_timer_start(self.ctx))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._ck(self.L.mhd_timer_stop(self.ctx, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: bool) -> None:
+        self._ck(self.L.mhd_profile(self.ctx, int(enable)))
+
+    def profile_read(self) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_longlong()
+        self._ck(self.L.mhd_profile_read(self.ctx, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def sync(self) -> None:
+        self._ck(self.L.mhd_sync(self.ctx))
+
+    def diagnostics(self, check: bool = True) -> dict:
+        d = abi.MhdDiag()
+        st = self.L.mhd_diagnostics(self.ctx, C.byref(d))
+        if check:
+            self._ck(st)
+        return d.as_dict()

@@ -1,0 +1,113 @@
+"""The fused FP64 path (one pass per RK3 substage, FMA on) against the
+oracle.  Tolerance: 1e-12 of each field's max-norm after one step; the
+drift after N steps is bounded and printed."""
+import itertools
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_util import oracle_for, rel_err, sim_from_fixture
+from mhd_gb300.case import Case, STATE_FIELDS, config0, initial_state, small_cases
+from mhd_gb300.sim import Simulation
+
+pytestmark = pytest.mark.gpu
+TOL_ONE_STEP = 1e-12
+
+
+def run_pair(case, nsteps, st=None):
+    st = initial_state(case) if st is None else st
+    sim = Simulation(case, path="fused")
+    sim.upload_state(st)
+    sim.communicate()
+    for _ in range(nsteps):
+        sim.step(case.dt)
+    o = oracle_for(case, st)
+    o.steps(nsteps)
+    got = sim.download_state()
+    sim.close()
+    return got, o
+
+
+SWITCHES = list(itertools.product([True, False], [True, False], [True, False]))
+
+
+@pytest.mark.parametrize("mag,rot,shr", SWITCHES)
+def test_one_step_all_switch_sets(mag, rot, shr):
+    base = small_cases()["mhd_fixedT"]
+    case = base.replace(lMag=mag, lRot=rot, lShr=shr, ANG=0.3, nPx=20, nPy=12, nPz=10)
+    got, o = run_pair(case, 1)
+    for k in STATE_FIELDS[:case.nfields]:
+        e = rel_err(got[k], o.arr[k])
+        assert e <= TOL_ONE_STEP, (k, e)
+
+
+@pytest.mark.parametrize("name", sorted(small_cases()))
+def test_one_step_boundary_variants(name):
+    case = small_cases()[name]
+    got, o = run_pair(case, 1)
+    for k in STATE_FIELDS[:case.nfields]:
+        assert rel_err(got[k], o.arr[k]) <= TOL_ONE_STEP, k
+
+
+def test_ghost_images_bit_exact_after_fused_steps():
+    case = small_cases()["mhd_rot_shr"].replace(nPx=40, nPy=9)
+    sim = Simulation(case, path="fused")
+    sim.upload_state(initial_state(case))
+    sim.communicate()
+    sim.steps(2, case.dt)
+    for k in STATE_FIELDS:
+        a = sim.download(k)[1:-1]
+        assert np.array_equal(a[:, 0, :], a[:, -2, :]) and np.array_equal(a[:, -1, :], a[:, 1, :]), k
+        assert np.array_equal(a[:, :, 0], a[:, :, -2]) and np.array_equal(a[:, :, -1], a[:, :, 1]), k
+    sim.close()
+
+
+@pytest.mark.parametrize("shape", [(33, 5, 4), (64, 16, 6), (7, 31, 5), (96, 48, 8)])
+def test_ragged_sizes(shape):
+    nx, ny, nz = shape
+    case = small_cases()["mhd_rot_shr"].replace(nPx=nx, nPy=ny, nPz=nz)
+    got, o = run_pair(case, 1)
+    for k in STATE_FIELDS:
+        assert rel_err(got[k], o.arr[k]) <= TOL_ONE_STEP, k
+
+
+def test_config0_drift_100_steps(capsys):
+    """Plain-method configuration 64x64x32, 100 steps: fused vs oracle."""
+    case = config0()
+    got, o = run_pair(case, 100)
+    errs = {k: rel_err(got[k], o.arr[k]) for k in STATE_FIELDS}
+    with capsys.disabled():
+        print("\nconfig0 100-step fused-vs-oracle relative max error:",
+              {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v <= 1e-9, (k, v)
+
+
+def test_diagnostics_and_cfl():
+    case = small_cases()["mhd_fixedT"]
+    st = initial_state(case)
+    sim = Simulation(case, path="fused")
+    sim.upload_state(st)
+    sim.communicate()
+    d0 = sim.diagnostics()
+    assert d0["flags"] == 0 and d0["total_mass"] > 0
+    o = oracle_for(case, st)
+    dt_o, um_o = o.cfl_dt()
+    dt_g, um_g = sim.cfl_dt()
+    assert dt_g == dt_o and um_g == um_o
+    sim.close()
+
+
+def test_nan_state_is_reported():
+    case = small_cases()["mhd_fixedT"]
+    st = initial_state(case)
+    st["TT"][3, 3, 3] = np.nan
+    sim = Simulation(case, path="fused")
+    sim.upload_state(st)
+    d = sim.diagnostics(check=False)
+    assert d["flags"] & 1
+    from mhd_gb300.abi import MhdError
+    with pytest.raises(MhdError):
+        sim.diagnostics()
+    sim.close()
