@@ -269,7 +269,10 @@ def run_ours(args, dist: Dist) -> None:
     hbm_peak = hbm_peak or 6800.0
     fp64_peak = C.c_double(0.0)
     abi.check(L.mhd_fp64_peak(C.byref(fp64_peak)))
-    fp64_flops_cell_substage = FP64_FLOPS_PER_CELL_SUBSTAGE.get((case.lMag, case.lRot, case.lShr))
+    key = (case.lMag, case.lRot, case.lShr)
+    inst_cell = FP64_INST_PER_CELL_SUBSTAGE.get(key)
+    tr = TRAFFIC_OVER_ALGORITHMIC.get(key)
+    traffic = per_launch_bytes * tr if tr else None
 
     # end to end through the C ABI with pinned host buffers
     nf = case.nfields
@@ -314,17 +317,18 @@ def run_ours(args, dist: Dist) -> None:
                 "path": "mhd_upload_state + mhd_step + mhd_download_state, pinned host memory"},
         "gpu_launches": 6 * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": TRAFFIC_PER_LAUNCH.get(args.config),
+                     "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                     "traffic_note": "ncu dram read+write of one launch at 256x256x128, scaled per cell",
                      "kernel": "k_substage (fused RK3 substage)", "peak_source": f"{peak_src} hbm_gbs",
                      "algorithmic_bytes_per_cell_step": bytes_cell_step,
                      "avg_launch_ms": 1e3 * avg_launch_s, "launches": launches},
-        "fp64": {"peak_tflops_measured": fp64_peak.value,
-                 "flops_per_cell_substage": fp64_flops_cell_substage,
-                 "achieved_tflops": (fp64_flops_cell_substage * case.cells / avg_launch_s / 1e12
-                                     if fp64_flops_cell_substage else None),
-                 "frac": (fp64_flops_cell_substage * case.cells / avg_launch_s / 1e12 / fp64_peak.value
-                          if fp64_flops_cell_substage and fp64_peak.value > 0 else None),
-                 "note": "the FP64 pipe, not HBM, bounds the fused FP64 kernel on GB300"},
+        "fp64": {"bound": "fp64 pipe", "unit": "G FP64 inst/s",
+                 "achieved": inst_cell * case.cells / avg_launch_s / 1e9 if inst_cell else None,
+                 "peak": fp64_peak.value * 1e3 / 2.0,
+                 "frac": (inst_cell * case.cells / avg_launch_s / 1e9) / (fp64_peak.value * 1e3 / 2.0)
+                         if inst_cell and fp64_peak.value > 0 else None,
+                 "inst_per_cell_substage": inst_cell, "peak_tflops_measured": fp64_peak.value,
+                 "note": "the FP64 pipe (measured DFMA roof), not HBM, bounds the fused FP64 kernel on GB300"},
         "clocks": clk,
     }
     if cpu:
@@ -332,11 +336,14 @@ def run_ours(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
-# FP64 flops per interior cell per substage of the fused kernel, from ncu's
-# dadd/dmul/dfma instruction counts (see profiles/); None until measured.
-FP64_FLOPS_PER_CELL_SUBSTAGE: dict = {}
-# dram__bytes_read.sum + dram__bytes_write.sum per k_substage launch, from ncu.
-TRAFFIC_PER_LAUNCH: dict = {}
+# FP64-pipe instructions per interior cell per substage of the fused kernel,
+# keyed by (lMag, lRot, lShr): ncu's sm__inst_executed_pipe_fp64 share x the
+# 2/clk/SM pipe rate x elapsed cycles / cells, from the 256x256x128 capture in
+# profiles/k_substage_fp64_config1physics_256x256x128.md.
+FP64_INST_PER_CELL_SUBSTAGE: dict = {(True, True, True): 295.0}
+# DRAM traffic over algorithmic bytes of one k_substage launch, measured by ncu
+# at 256x256x128 (2.270 GB / 2.282 GB); applied to the full-size average launch.
+TRAFFIC_OVER_ALGORITHMIC = {(True, True, True): 2.270 / 2.282}
 
 
 def main():
