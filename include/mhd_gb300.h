@@ -146,6 +146,41 @@ int mhd_communicate(mhd_ctx* ctx);              /* communicate(), 3dmhdmpi.h:11-
 /* CFL time step of step() (3dmhdsub.h:36-106); blocks until known. */
 int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach);
 
+/* ---- right-hand sides without any allocation ---------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a service that reserved its HBM up front in its own pool, or a loop that
+ * must not hit cudaMalloc's implicit device synchronisation): computes the
+ * same right-hand sides as mhd_fluxes, bit for bit, on device buffers the
+ * caller owns, and allocates nothing.  Its scratch is a fixed device array
+ * of MHD_NOALLOC_MAX_CELLS x 5 doubles (15.7 MB) inside the library, held by
+ * every GPU that loads it until the process exits; grids with more than
+ * MHD_NOALLOC_MAX_CELLS cells (ghosts included) are rejected with
+ * MHD_ERR_INVALID and a message on stderr.  The first call on a device looks
+ * up the array's address (make it before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller.  Inputs are not modified (RO is only read; the reference
+ * inverts it in place).  With lShr, flux[MHD_FT - 8] is read and accumulated,
+ * as the reference's FT is. */
+#define MHD_NOALLOC_MAX_CELLS 393216
+typedef struct mhd_fluxes_noalloc_args {
+    int nPx, nPy, nPz;
+    unsigned switches;
+    int izCon, iTCon, iBCon;
+    int reserved_i;
+    double RE, PR, THETA, GRAV, RY, ANG, RM, BETA, TP, GAMMA, SFF, TB;
+    /* device pointers: metric arrays of nx / ny / nz doubles */
+    const double *dxxdx, *d2xxdx2, *DDX;
+    const double *dyydy, *d2yydy2, *DDY;
+    const double *dzzdz, *d2zzdz2, *DDZ;
+    const double *RKAPA, *DKAPA;
+    /* device pointers, nz*ny*nx doubles each, in field-id order:
+     * state RU RV RW TT RO BX BY BZ (ghosts filled), flux FU FV FW FR FT WW1 WW2 WW3;
+     * the B fields and WW1..3 may be NULL without lMag */
+    const double* state[8];
+    double* flux[8];
+} mhd_fluxes_noalloc_args;
+int mhd_fluxes_noalloc(const mhd_fluxes_noalloc_args* args, void* stream);
+
 /* ---- fused time stepping ------------------------------------------------ */
 /* One RK3 step, replacing step() (3dmhdsub.h:31-153).  dt > 0: fixed step;
  * dt <= 0: the reference's CFL step (then the call blocks for the dt).

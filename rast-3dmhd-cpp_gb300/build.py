@@ -27,6 +27,7 @@ UNITS = {
     "mhd_parity.cu": ["-fmad=false"],
     "mhd_fused.cu": [],
     "mhd_diag.cu": [],
+    "mhd_noalloc.cu": [],
 }
 
 

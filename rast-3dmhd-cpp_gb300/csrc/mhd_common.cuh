@@ -66,6 +66,10 @@ struct Coefs {
 // Parity path (compiled with -fmad=false, bit-exact with the reference).
 int parity_fluxes(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* P, double* UU,
                   double* VV, double* WW, cudaStream_t st);
+// The same right-hand sides with 1/rho written to RI instead of RO (RO is
+// only read); every scratch array is fully written before it is read.
+int parity_fluxes_ext(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* RI, double* P,
+                      double* UU, double* VV, double* WW, cudaStream_t st);
 int parity_rk(int kind, int nf, const Grid& g, Fields8 U, Fields8 Z, Fields8 F, double coef, cudaStream_t st);
 int parity_bcon(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
 int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st);

@@ -78,6 +78,26 @@ __global__ void k_prep(Grid g, Consts c, Fields8 U, double* FW, double* P, doubl
     }
 }
 
+// As k_prep, but 1/rho goes to separate scratch and RO is left as it was.
+__global__ void k_prep_ext(Grid g, Consts c, Fields8 U, double* RI, double* FW, double* P, double* UU, double* VV,
+                           double* WW) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx);
+        const int y = (int)((i / g.nx) % g.ny);
+        const int z = (int)(i / g.sz);
+        const double ro = U.p[S_RO][i];
+        if (x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1) FW[i] = ro * c.GRAV;
+        P[i] = ro * U.p[S_TT][i];
+        const double ri = 1.0 / ro;
+        RI[i] = ri;
+        UU[i] = U.p[S_RU][i] * ri;
+        VV[i] = U.p[S_RV][i] * ri;
+        WW[i] = U.p[S_RW][i] * ri;
+    }
+}
+
 template <class SW>
 __global__ void k_flux(Grid g, Consts c, Fields8 U, Fields8 F, const double* __restrict__ P,
                        const double* __restrict__ UU, const double* __restrict__ VV, const double* __restrict__ WW) {
@@ -543,6 +563,16 @@ int parity_fluxes(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields
     const long long n = (long long)g.nx * g.ny * g.nz;
     k_prep<<<grid_for(n, 256, 152 * 32), 256, 0, st>>>(g, c, U, F.p[F_FW], P, UU, VV, WW);
     MHD_DISPATCH_SW(sw, launch_flux, g, c, U, F, P, UU, VV, WW, st);
+    return (int)cudaGetLastError();
+}
+
+int parity_fluxes_ext(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fields8 F, double* RI, double* P,
+                      double* UU, double* VV, double* WW, cudaStream_t st) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    k_prep_ext<<<grid_for(n, 256, 152 * 32), 256, 0, st>>>(g, c, U, RI, F.p[F_FW], P, UU, VV, WW);
+    Fields8 V = U;
+    V.p[S_RO] = RI;  // k_flux reads 1/rho through the RO slot
+    MHD_DISPATCH_SW(sw, launch_flux, g, c, V, F, P, UU, VV, WW, st);
     return (int)cudaGetLastError();
 }
 

@@ -55,6 +55,19 @@ class MhdDiag(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+NOALLOC_MAX_CELLS = 393216
+
+
+class MhdFluxesNoallocArgs(C.Structure):
+    _fields_ = [("nPx", C.c_int), ("nPy", C.c_int), ("nPz", C.c_int), ("switches", C.c_uint),
+                ("izCon", C.c_int), ("iTCon", C.c_int), ("iBCon", C.c_int), ("reserved_i", C.c_int)] + \
+               [(n, C.c_double) for n in ("RE", "PR", "THETA", "GRAV", "RY", "ANG", "RM", "BETA", "TP", "GAMMA",
+                                           "SFF", "TB")] + \
+               [(n, C.c_void_p) for n in ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2",
+                                          "DDZ", "RKAPA", "DKAPA")] + \
+               [("state", C.c_void_p * 8), ("flux", C.c_void_p * 8)]
+
+
 class MhdError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
@@ -94,6 +107,7 @@ SIGNATURES = {
     "mhd_profile": [C.c_void_p, C.c_int],
     "mhd_profile_read": [C.c_void_p, _DP, C.POINTER(C.c_longlong)],
     "mhd_fp64_peak": [_DP],
+    "mhd_fluxes_noalloc": [C.POINTER(MhdFluxesNoallocArgs), C.c_void_p],
     "mhd_host_alloc": [C.c_size_t, C.POINTER(C.c_void_p)],
     "mhd_host_free": [C.c_void_p],
 }
