@@ -43,7 +43,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
 
 from mhd_gb300 import abi  # noqa: E402
-from mhd_gb300.case import STATE_FIELDS, config0, config1, initial_state  # noqa: E402
+from mhd_gb300.case import STATE_FIELDS, config0, config1, config2_batch, config3, initial_state  # noqa: E402
 
 METRIC = "cell-RK3-updates/s"
 # Algorithmic HBM traffic of the fused FP64 path per interior cell and RK3
@@ -340,10 +340,149 @@ def run_ours(args, dist: Dist) -> None:
 # keyed by (lMag, lRot, lShr): ncu's sm__inst_executed_pipe_fp64 share x the
 # 2/clk/SM pipe rate x elapsed cycles / cells, from the 256x256x128 capture in
 # profiles/k_substage_fp64_config1physics_256x256x128.md.
-FP64_INST_PER_CELL_SUBSTAGE: dict = {(True, True, True): 295.0}
+FP64_INST_PER_CELL_SUBSTAGE: dict = {(True, True, True): 256.5}
 # DRAM traffic over algorithmic bytes of one k_substage launch, measured by ncu
-# at 256x256x128 (2.270 GB / 2.282 GB); applied to the full-size average launch.
-TRAFFIC_OVER_ALGORITHMIC = {(True, True, True): 2.270 / 2.282}
+# at 256x256x128 (2.274 GB / 2.282 GB); applied to the full-size average launch.
+TRAFFIC_OVER_ALGORITHMIC = {(True, True, True): 2.274 / 2.282}
+
+
+# ---------------------------------------------------------------------------
+# precision form: FP32 storage vs the FP64 path on the 256x256x128 case
+# ---------------------------------------------------------------------------
+def run_precision(args, dist: Dist) -> None:
+    from mhd_gb300.sim import Simulation
+    L = abi.load()
+    abi.check(L.mhd_set_device(dist.local))
+    case = config3()
+    nsteps = args.precision_steps
+    st = initial_state(case)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        sim = Simulation(case, precision=prec)
+        sim.upload_state(st)
+        sim.communicate()
+        d0 = sim.diagnostics()
+        for _ in range(3):
+            sim.step(case.dt)
+        sim.upload_state(st)
+        sim.communicate()
+        sim.set_time(0.0, 0)
+        sim.sync()
+        sim.profile(True)
+        sim.timer_start()
+        sim.steps(nsteps, case.dt)
+        ms = sim.timer_stop()
+        sub_ms, launches = sim.profile_read()
+        sim.profile(False)
+        d1 = sim.diagnostics(check=False)
+        res[prec] = {"state": sim.download_state(), "ms": ms, "sub_ms": sub_ms, "launches": launches,
+                     "d0": d0, "d1": d1}
+        sim.close()
+    errs = {}
+    for k in STATE_FIELDS:
+        a = res["fp32"]["state"][k][1:-1, 1:-1, 1:-1]
+        b = res["fp64"]["state"][k][1:-1, 1:-1, 1:-1]
+        nb = np.linalg.norm(b)
+        errs[k] = {"l2_rel": float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b)),
+                   "linf_rel": float(np.abs(a - b).max() / np.abs(b).max()) if np.abs(b).max() > 0 else None}
+    out = {"form": "precision", "metric": METRIC, "unit": METRIC, "steps": nsteps,
+           "config": {"workload": f"{case.name}: lMag, noise 1e-2, dt {case.dt}, {nsteps} steps"}}
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    for prec in ("fp64", "fp32"):
+        r = res[prec]
+        bytes_cs = 640.0 if prec == "fp64" else 448.0
+        avg = r["sub_ms"] / 1e3 / max(r["launches"], 1)
+        out[prec] = {"value": case.cells * nsteps / (r["ms"] / 1e3), "ms_per_step": r["ms"] / nsteps,
+                     "algorithmic_bytes_per_cell_step": bytes_cs,
+                     "substage_gbs": case.cells * bytes_cs / 3 / avg / 1e9,
+                     "substage_hbm_frac": case.cells * bytes_cs / 3 / avg / 1e9 / hbm,
+                     "drift": {k: r["d1"][k] / r["d0"][k] - 1.0 if r["d0"][k] else None
+                               for k in ("total_mass", "total_energy")},
+                     "max_divb": [r["d0"]["max_divb"], r["d1"]["max_divb"]]}
+    out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["errors_fp32_vs_fp64"] = errs
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# batching form: 64 uneven instances, persistent launch per substage, graphs
+# ---------------------------------------------------------------------------
+def run_batch(args, dist: Dist) -> None:
+    from mhd_gb300.sim import Batch, Simulation
+    L = abi.load()
+    abi.check(L.mhd_set_device(dist.local))
+    cases = config2_batch()
+    nsteps = args.batch_steps
+    sims = []
+    for c in cases:
+        s = Simulation(c)
+        s.upload_state(initial_state(c))
+        s.communicate()
+        sims.append(s)
+    cells = sum(c.cells for c in cases)
+    b = Batch(sims)
+    chosen, tile_ms = b.autotune()
+    b.steps(3)
+    b.sync()
+    sims[0].timer_start()
+    t = time.perf_counter()
+    b.steps(nsteps)
+    b.sync()
+    secs = time.perf_counter() - t
+    b.close()
+    # the plain single-instance path, instance after instance (a bounded sample of steps)
+    serial_steps = max(1, min(nsteps, args.serial_steps))
+    for s in sims:
+        s.steps(2, s.case.dt)
+        s.sync()
+    t = time.perf_counter()
+    for s in sims:
+        s.steps(serial_steps, s.case.dt)
+        s.sync()
+    serial_secs = (time.perf_counter() - t) * nsteps / serial_steps
+    for s in sims:
+        s.close()
+    out = {"form": "batch", "metric": METRIC, "unit": METRIC, "instances": len(cases), "steps": nsteps,
+           "cells_per_step": cells, "dtype": "f64",
+           "value": cells * nsteps / secs, "ms_per_step": 1e3 * secs / nsteps,
+           "autotune": {"chosen": ["32x4", "32x8", "16x8"][chosen], "ms_per_step_by_tile": tile_ms},
+           "plain_serial": {"value": cells * nsteps / serial_secs, "ms_per_step": 1e3 * serial_secs / nsteps,
+                            "sample_steps": serial_steps},
+           "speedup_vs_plain_serial": serial_secs / secs,
+           "config": {"workload": "64 FP64 MHD instances, nx=ny in {32,48,64,96,128}, nz in {32,64}, "
+                                  "1/Re log-uniform [3e-3,3e-2], Bz0 log-uniform [1e-4,1e-2]"}}
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# serving form: Poisson request stream, continuous batching under an HBM budget
+# ---------------------------------------------------------------------------
+def run_serve(args, dist: Dist) -> None:
+    from mhd_gb300.serve import Server, poisson_requests, run_serial
+    L = abi.load()
+    abi.check(L.mhd_set_device(dist.local))
+    n = args.serve_requests
+    smin, smax = max(1, 50 // args.serve_step_scale), max(2, 2000 // args.serve_step_scale)
+    reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
+    srv = Server(150 << 30, quantum=25)
+    st = srv.run(reqs, realtime=True)
+    # baseline: the same requests one after another on the plain FP64 path
+    serial_reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
+    base = run_serial(serial_reqs)
+    out = {"form": "serve", "metric": METRIC, "unit": METRIC, "requests": n, "rate_per_s": 20.0,
+           "steps_range": [smin, smax], "hbm_budget_gb": 150,
+           "value": st["value"], "wall_s": st["wall_s"], "tts_p50_s": st["tts_p50_s"],
+           "tts_p99_s": st["tts_p99_s"], "max_resident": st["max_resident"], "tile": st["tile"],
+           "batch_rebuilds": st["batch_rebuilds"],
+           "serial_plain_fp64": base, "throughput_vs_serial": st["value"] / base["value"],
+           "config": {"workload": f"Poisson stream of {n} simulations at 20/s, grids log-uniform 32^3..256^2x128, "
+                                  f"steps uniform [{smin},{smax}] (the configured [50,2000] / "
+                                  f"{args.serve_step_scale}), half FP32 storage, random seeds and 1/Re"}}
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def main():
@@ -354,6 +493,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=["config1", "config0", "mid"], default="config1")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--form", choices=["plain", "precision", "batch", "serve"], default="plain")
+    ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--serial-steps", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-step-scale", type=int, default=10)
+    ap.add_argument("--precision-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -361,6 +506,12 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.form == "precision":
+            run_precision(args, dist)
+        elif args.form == "batch":
+            run_batch(args, dist)
+        elif args.form == "serve":
+            run_serve(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -133,8 +133,28 @@ int mhd_download(mhd_ctx* ctx, int field, double* host);
  * contiguous host block of nfields * nz*ny*nx doubles in field-id order. */
 int mhd_upload_state(mhd_ctx* ctx, const double* host);
 int mhd_download_state(mhd_ctx* ctx, double* host);
+/* Synthetic initial state written on the device, without host arrays
+ * (the reference builds its state on the host in Static(),
+ * 3dmhdphsic.h:549-763): polytrope T = 1 + THETA z, rho = T^m with
+ * m = GRAV/THETA - 1, interior T *= 1 + noise N(0,1) with N from splitmix64 of
+ * (seed, interior cell index) through Box-Muller, Bz = bz0 on interior planes,
+ * zero momenta (lShr: rho v = +-rho on the walls), periodic x/y ghosts.
+ * zcoord: host array of nz depths.  FP64 contexts; blocks until done. */
+int mhd_init_polytrope(mhd_ctx* ctx, const double* zcoord, double noise, unsigned long long seed, double bz0);
 /* Simulation time and step counter (TIMT, nIt). */
 int mhd_set_time(mhd_ctx* ctx, double timt, long long nit);
+
+/* Dump files in the reference's layout (dumpData / loadData, 3dmhdio.h:20-72):
+ * for an nPEy x nPEz rank grid, "<prefix>.dat0.PPPP" per rank holds record idx
+ * of RU RV RW TT RO [BX BY BZ], each the rank's interior block x fastest.
+ * `state` is nfields host arrays of nz*ny*nx doubles in field-id order (as
+ * mhd_download_state fills it); reading fills the interior only (call
+ * mhd_communicate after uploading).  Writing keeps earlier records of the
+ * file, which the reference's writer truncates.  Host code, no GPU needed. */
+int mhd_write_dat0(const char* prefix, int nPx, int nPy, int nPz, int nfields, const double* state, int nPEy,
+                   int nPEz, int idx);
+int mhd_read_dat0(const char* prefix, int nPx, int nPy, int nPz, int nfields, double* state, int nPEy, int nPEz,
+                  int idx);
 
 /* ---- unfused parity ABI: one call per reference function ---------------- */
 int mhd_fluxes(mhd_ctx* ctx);                   /* fluxes(FORRANGE), 3dmhdsub.h:194-696 */
@@ -191,6 +211,27 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt);
 /* Mass, energy, max|div B| and sanity flags of the current state (blocks). */
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
 int mhd_sync(mhd_ctx* ctx);
+
+/* ---- ragged batches ------------------------------------------------------ */
+/* n independent FP64 instances (fused-path contexts with one switch set, any
+ * sizes) stepped together: each RK3 substage is one persistent launch over
+ * the tiles of all instances, the whole step is a CUDA graph, and the tile
+ * shape is picked by timing every candidate on a scratch copy of the batch
+ * (cached per batch signature).  No counterpart in the reference, which runs
+ * one instance per MPI job.  Results equal each instance stepped alone with
+ * the same tile shape, bit for bit.  The batch orders itself after work
+ * already queued on the instances' streams, and their later work after it. */
+typedef struct mhd_batch mhd_batch;
+int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* stream, mhd_batch** out);
+int mhd_batch_destroy(mhd_batch* b);
+/* tile shape: -1 = autotune on the next step, 0 = 32x4, 1 = 32x8, 2 = 16x8 */
+int mhd_batch_set_tile(mhd_batch* b, int tile);
+int mhd_batch_tile(const mhd_batch* b, int* tile);
+/* Time every tile shape (ms_per_step, may be NULL, gets one entry per shape)
+ * and keep the fastest. */
+int mhd_batch_autotune(mhd_batch* b, int* chosen, double* ms_per_step);
+int mhd_batch_steps(mhd_batch* b, int nsteps);
+int mhd_batch_sync(mhd_batch* b);
 
 /* ---- device selection and timing ---------------------------------------- */
 /* Make `device` current for this thread's later mhd_* calls (one process per

@@ -17,6 +17,8 @@
  *           without its CFL section
  *   mode 2  N calls of the reference step() itself      (3dmhdsub.h:31-153)
  *   mode 3  one RK3 substage                            (3dmhdsub.h:116-124)
+ *   mode 4  as mode 1, then the reference's dumpData() writes record 0 of
+ *           "<argv[3]>.dat0.PPPP" per rank                (3dmhdio.h:20-35)
  * and every rank writes the part of the global arrays it owns into the
  * output file, so the output is the single-domain equivalent state.
  */
@@ -217,6 +219,13 @@ int main(int argc, char** argv) {
             step();
             dt_hist.push_back(DT);
         }
+    } else if (h.mode == 4) {
+        if (argc < 4) die("mode 4 needs a dump prefix");
+        for (int n = 0; n < nsteps; n++) {
+            fixed_dt_step();
+            dt_hist.push_back(DT);
+        }
+        dumpData(std::string(argv[3]) + ".dat0." + PEextn(), 0);
     } else if (h.mode == 3) {
         step_block_ZETA0(FORRANGE);
         fluxes(FORRANGE);

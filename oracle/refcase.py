@@ -168,7 +168,7 @@ def build(case: Case) -> Path:
 # ---------------------------------------------------------------------------
 # harness input / output files
 # ---------------------------------------------------------------------------
-MODES = {"fluxes": 0, "steps": 1, "cfl": 2, "substage": 3}
+MODES = {"fluxes": 0, "steps": 1, "cfl": 2, "substage": 3, "dump": 4}
 
 
 def write_input(path: Path, case: Case, state: dict, mode: str, nsteps: int,
@@ -204,15 +204,17 @@ def read_output(path: Path, case: Case, nsteps: int) -> dict:
 
 
 def run(case: Case, state: dict, mode: str = "steps", nsteps: int = 1,
-        FT: np.ndarray | None = None, timt0: float = 0.0, timeout: float = 1800.0) -> dict:
-    """Run the reference on ``state`` and return the gathered global arrays."""
+        FT: np.ndarray | None = None, timt0: float = 0.0, timeout: float = 1800.0,
+        dump_prefix: str | None = None) -> dict:
+    """Run the reference on ``state`` and return the gathered global arrays.
+    mode "dump" also has the reference write its own dump files at dump_prefix."""
     exe = build(case)
     with tempfile.TemporaryDirectory(prefix="mhdref_") as td:
         fin = Path(td) / "in.bin"
         fout = Path(td) / "out.bin"
         write_input(fin, case, state, mode, nsteps, FT=FT, timt0=timt0)
-        r = subprocess.run([str(exe), str(fin), str(fout)], capture_output=True, text=True,
-                           timeout=timeout, cwd=td)
+        cmd = [str(exe), str(fin), str(fout)] + ([dump_prefix] if dump_prefix else [])
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout, cwd=td)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}):\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
         return read_output(fout, case, nsteps)

@@ -22,13 +22,20 @@ OBJ = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++20", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", str(PKG.parent / "include")]
-UNITS = {
-    "mhd_abi.cu": [],
-    "mhd_parity.cu": ["-fmad=false"],
-    "mhd_fused.cu": [],
-    "mhd_diag.cu": [],
-    "mhd_noalloc.cu": [],
-}
+# (source, object name, extra flags)
+UNITS = [
+    ("mhd_abi.cu", "mhd_abi", []),
+    ("mhd_parity.cu", "mhd_parity", ["-fmad=false"]),
+    ("mhd_fused.cu", "mhd_fused", []),
+    ("mhd_fused_batch.cu", "mhd_fused_batch_uxy", ["-DMHD_BATCH_UXY=1"]),
+    ("mhd_fused_batch.cu", "mhd_fused_batch_gen", ["-DMHD_BATCH_UXY=0"]),
+    ("mhd_diag.cu", "mhd_diag", []),
+    ("mhd_noalloc.cu", "mhd_noalloc", []),
+    ("mhd_fp32.cu", "mhd_fp32", []),
+    ("mhd_batch.cu", "mhd_batch", []),
+    ("mhd_io.cu", "mhd_io", []),
+    ("mhd_init.cu", "mhd_init", []),
+]
 
 
 def nvcc() -> str:
@@ -50,13 +57,13 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "mhd_gb300.h"]
     jobs = []
-    for src, extra in UNITS.items():
+    for src, oname, extra in UNITS:
         s = CSRC / src
-        o = OBJ / (s.stem + ".o")
+        o = OBJ / (oname + ".o")
         if _stale(o, [s] + headers) or ptxas_info:
             cmd = [nvcc()] + ARCH + COMMON + extra + (["-Xptxas", "-v"] if ptxas_info else []) + \
                   ["-c", str(s), "-o", str(o)]
-            jobs.append((src, cmd))
+            jobs.append((oname, cmd))
 
     def run(job):
         name, cmd = job
@@ -70,7 +77,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
                     sys.stderr.write(r.stderr)
                 if r.returncode != 0:
                     raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr[-6000:]}")
-    objs = [OBJ / (Path(s).stem + ".o") for s in UNITS]
+    objs = [OBJ / (oname + ".o") for _, oname, _ in UNITS]
     if _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp%d" % os.getpid())
         cmd = [nvcc()] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs]

@@ -10,8 +10,7 @@
 //          across substages)
 //   S      scratch of the unfused path: p = rho*T and the velocities
 // Buffers that a call sequence never needs are allocated on first use.
-#include "../../include/mhd_gb300.h"
-#include "mhd_common.cuh"
+#include "mhd_context.h"
 
 #include <cmath>
 #include <cstdio>
@@ -21,38 +20,8 @@
 
 using namespace mhd;
 
-struct mhd_ctx {
-    mhd_params prm{};
-    mhd_constants k{};
-    Grid g{};
-    Consts c{};
-    Coefs coef{};
-    unsigned sw = 0;
-    int nf = 5;
-    size_t ncell = 0;  // nx*ny*nz
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    double* d_metric = nullptr;  // 11 metric arrays + 9 coefficient arrays
-    double* U[2] = {nullptr, nullptr};
-    int cur = 0;
-    double* Zb = nullptr;
-    double* Fb = nullptr;
-    double* Sb = nullptr;
-    double* red = nullptr;   // reduction partials
-    double* d_out = nullptr; // 8 doubles of reduction results
-    double* h_out = nullptr; // pinned mirror of d_out
-    int red_blocks = 0;
-    bool ghosts_synced = false;  // z ghost planes of U[1-cur] match U[cur]
-    double timt = 0.0;
-    long long nit = 0;
-    double last_dt = 0.0, last_umach = 0.0;
-    size_t bytes = 0;
-    std::string err;
-    cudaEvent_t t0 = nullptr, t1 = nullptr;
-    bool profiling = false;
-    std::vector<cudaEvent_t> prof_events;  // pairs around each substage launch
-    size_t prof_used = 0;
-};
+
+
 
 namespace {
 
@@ -139,7 +108,9 @@ int validate(const mhd_params* p, std::string& why) {
     if ((p->iTCon == 0 || p->iTCon == 1) && p->TP != 0.0)
         return why = "the plume upper boundary (TP != 0 with iTCon 0/1) is not built", MHD_ERR_UNSUPPORTED;
     if (p->iBCon != 0) return why = "iBCon must be 0", MHD_ERR_UNSUPPORTED;
-    if (p->precision != MHD_PREC_FP64) return why = "this context type stores FP64 state", MHD_ERR_UNSUPPORTED;
+    if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return why = "unknown precision", MHD_ERR_INVALID;
+    if (p->precision == MHD_PREC_FP32 && p->path != MHD_PATH_FUSED)
+        return why = "FP32 storage exists only on the fused path", MHD_ERR_UNSUPPORTED;
     if (p->path != MHD_PATH_FUSED && p->path != MHD_PATH_PARITY) return why = "unknown kernel path", MHD_ERR_INVALID;
     if (!(p->RE > 0) || !(p->RM > 0) || !(p->BETA > 0) || !(p->PR > 0) || !(p->GAMMA > 1))
         return why = "RE, RM, BETA, PR must be > 0 and GAMMA > 1", MHD_ERR_INVALID;
@@ -229,7 +200,167 @@ int fused_step(mhd_ctx* ctx, double dt) {
     return MHD_OK;
 }
 
+int alloc_f32(mhd_ctx* ctx, float** p) {
+    if (*p) return MHD_OK;
+    const size_t b = ctx->ncell * sizeof(float) * 8;
+    cudaError_t e = cudaMalloc(p, b);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(ctx, MHD_ERR_NOMEM, "device allocation of " + std::to_string(b) + " bytes failed");
+    }
+    ctx->bytes += b;
+    e = cudaMemsetAsync(*p, 0, b, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync");
+    return MHD_OK;
+}
+
+Fields8f fields32_of(const mhd_ctx* c, float* base) {
+    Fields8f f{};
+    for (int k = 0; k < 8; k++) f.p[k] = base ? base + (size_t)k * c->ncell : nullptr;
+    return f;
+}
+
+// Profile of a state field in the FP32 layout: RO -> rho0, TT -> T0, others none.
+const double* profile_host(const mhd_ctx* c, int field) {
+    const int nz = c->g.nz;
+    if (field == MHD_RO) return c->h_bg.data();
+    if (field == MHD_TT) return c->h_bg.data() + nz;
+    return nullptr;
+}
+
+// rho0 / T0 := horizontal mean of the uploaded field over interior (y, x), per z;
+// for T0 also its premultiplied first and second z derivatives.
+int set_profile(mhd_ctx* ctx, int field, const double* host) {
+    const int nx = ctx->g.nx, ny = ctx->g.ny, nz = ctx->g.nz;
+    double* bg = ctx->h_bg.data() + (field == MHD_RO ? 0 : nz);
+    for (int z = 0; z < nz; z++) {
+        double s = 0.0;
+        for (int y = 1; y < ny - 1; y++)
+            for (int x = 1; x < nx - 1; x++) s += host[((size_t)z * ny + y) * nx + x];
+        bg[z] = s / ((double)(nx - 2) * (ny - 2));
+    }
+    if (field == MHD_TT) {
+        double* d1 = ctx->h_bg.data() + 2 * nz;
+        double* d2 = ctx->h_bg.data() + 3 * nz;
+        const double *cz1 = ctx->h_cz.data(), *cz2a = cz1 + nz, *cz2b = cz1 + 2 * nz;
+        for (int z = 0; z < nz; z++) {
+            d1[z] = d2[z] = 0.0;
+            if (z == 0 || z == nz - 1) continue;
+            const double p = bg[z + 1], m = bg[z - 1];
+            d1[z] = (p - m) * cz1[z];
+            d2[z] = (p - m) * cz2a[z] + (p + m - 2.0 * bg[z]) * cz2b[z];
+        }
+    }
+    CK(cudaMemcpy(ctx->d_bg, ctx->h_bg.data(), sizeof(double) * 4 * nz, cudaMemcpyHostToDevice));
+    return MHD_OK;
+}
+
+int upload32(mhd_ctx* ctx, int field, const double* host) {
+    if (field == MHD_RO || field == MHD_TT) {
+        int rc = set_profile(ctx, field, host);
+        if (rc) return rc;
+    }
+    const double* bg = profile_host(ctx, field);
+    const size_t plane = (size_t)ctx->g.sz;
+    std::vector<float> tmp(ctx->ncell);
+    for (size_t i = 0; i < ctx->ncell; i++) tmp[i] = (float)(host[i] - (bg ? bg[i / plane] : 0.0));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(ctx->U32[ctx->cur] + (size_t)field * ctx->ncell, tmp.data(), ctx->ncell * sizeof(float),
+                  cudaMemcpyHostToDevice));
+    // the FP64 register carries the full state between steps
+    CK(cudaMemcpy(ctx->Zb + (size_t)field * ctx->ncell, host, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->ghosts_synced = false;
+    return MHD_OK;
+}
+
+int download32(mhd_ctx* ctx, int field, double* host) {
+    std::vector<float> tmp(ctx->ncell);
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(tmp.data(), ctx->U32[ctx->cur] + (size_t)field * ctx->ncell, ctx->ncell * sizeof(float),
+                  cudaMemcpyDeviceToHost));
+    const double* bg = profile_host(ctx, field);
+    const size_t plane = (size_t)ctx->g.sz;
+    for (size_t i = 0; i < ctx->ncell; i++) host[i] = (double)tmp[i] + (bg ? bg[i / plane] : 0.0);
+    return MHD_OK;
+}
+
+int sync_zghosts32(mhd_ctx* ctx) {
+    if (ctx->ghosts_synced) return MHD_OK;
+    const size_t plane = (size_t)ctx->g.sz * sizeof(float);
+    float* a = ctx->U32[ctx->cur];
+    float* b = ctx->U32[1 - ctx->cur];
+    const size_t last = (size_t)(ctx->g.nz - 1) * ctx->g.sz;
+    for (int f = 0; f < 8; f++) {
+        float* fa = a + (size_t)f * ctx->ncell;
+        float* fb = b + (size_t)f * ctx->ncell;
+        CK(cudaMemcpyAsync(fb, fa, plane, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(fb + last, fa + last, plane, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ctx->ghosts_synced = true;
+    return MHD_OK;
+}
+
+int fused32_step(mhd_ctx* ctx, double dt) {
+    int rc = alloc_f32(ctx, &ctx->U32[1]);
+    if (rc) return rc;
+    if ((ctx->sw & kSwShr) && !ctx->FT64) {
+        rc = alloc_block(ctx, &ctx->FT64, 1);
+        if (rc) return rc;
+    }
+    rc = sync_zghosts32(ctx);
+    if (rc) return rc;
+    const int nz = ctx->g.nz;
+    const double gam[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
+    const double zet[3] = {ctx->k.ZETA1, ctx->k.ZETA2, 0.0};
+    for (int s = 0; s < 3; s++) {
+        Fused32Args a{};
+        a.g = ctx->g;
+        a.c = ctx->c;
+        a.k = ctx->coef;
+        a.U = fields32_of(ctx, ctx->U32[ctx->cur]);
+        a.Uo = fields32_of(ctx, ctx->U32[1 - ctx->cur]);
+        a.Z = fields_of(ctx, ctx->Zb);
+        a.FT = ctx->FT64;
+        a.bgR = ctx->d_bg;
+        a.bgT = ctx->d_bg + nz;
+        a.dzT0 = ctx->d_bg + 2 * nz;
+        a.d2zT0 = ctx->d_bg + 3 * nz;
+        a.gdt = gam[s] * dt;
+        a.zdt = zet[s] * dt;
+        a.substage = s;
+        cudaEvent_t* ev = nullptr;
+        if (ctx->profiling) {
+            if (ctx->prof_used + 2 > ctx->prof_events.size()) {
+                for (int j = 0; j < 64; j++) {
+                    cudaEvent_t e0;
+                    CK(cudaEventCreate(&e0));
+                    ctx->prof_events.push_back(e0);
+                }
+            }
+            ev = &ctx->prof_events[ctx->prof_used];
+            ctx->prof_used += 2;
+            CK(cudaEventRecord(ev[0], ctx->stream));
+        }
+        int e = fused32_substage(ctx->sw, a, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 substage launch");
+        if (ev) CK(cudaEventRecord(ev[1], ctx->stream));
+        e = fused32_bcon_ghost(ctx->sw, ctx->g, ctx->c, a.Uo, a.Z, a.bgR, a.bgT, ctx->timt, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 BCON launch");
+        ctx->cur = 1 - ctx->cur;
+    }
+    return MHD_OK;
+}
+
 }  // namespace
+
+namespace mhd::ctxops {
+int ensure_u1(mhd_ctx* ctx) { return ::ensure_u1(ctx); }
+int sync_zghosts(mhd_ctx* ctx) { return ::sync_zghosts(ctx); }
+int alloc_block(mhd_ctx* ctx, double** p, int nfields) { return ::alloc_block(ctx, p, nfields); }
+Fields8 fields_of(const mhd_ctx* c, double* base) { return ::fields_of(c, base); }
+int fail(mhd_ctx* c, int code, const std::string& msg) { return ::fail(c, code, msg); }
+}  // namespace mhd::ctxops
 
 extern "C" {
 
@@ -295,11 +426,28 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     const double* d1s[3] = {p.dxxdx, p.dyydy, p.dzzdz};
     const double* d2s[3] = {p.d2xxdx2, p.d2yydy2, p.d2zzdz2};
     const int ns[3] = {nx, ny, nz};
+    size_t base_off[3], scaled_off[3];
     for (int ax = 0; ax < 3; ax++) {
+        base_off[ax] = h.size();
         for (int i = 0; i < ns[ax]; i++) h.push_back(d1s[ax][i] * hs[ax]);
         for (int i = 0; i < ns[ax]; i++) h.push_back(d2s[ax][i] * hs[ax]);
         for (int i = 0; i < ns[ax]; i++) h.push_back(d1s[ax][i] * d1s[ax][i] * h2s[ax]);
     }
+    const double scales[3] = {ctx->k.ORE, ctx->k.ORE * ctx->k.C43, ctx->k.ORM};
+    for (int ax = 0; ax < 3; ax++) {
+        scaled_off[ax] = h.size();
+        for (int sc = 0; sc < 3; sc++) {
+            for (int i = 0; i < ns[ax]; i++) h.push_back(d2s[ax][i] * hs[ax] * scales[sc]);
+            for (int i = 0; i < ns[ax]; i++) h.push_back(d1s[ax][i] * d1s[ax][i] * h2s[ax] * scales[sc]);
+        }
+    }
+    const size_t kap_off = h.size();
+    const double tmpc = ctx->k.OCV / ctx->k.REPR;
+    for (int i = 0; i < nz; i++) h.push_back(tmpc * p.RKAPA[i]);
+    for (int i = 0; i < nz; i++) h.push_back(tmpc * p.DKAPA[i]);
+    bool uxy = true;
+    for (int i = 0; i < nx; i++) uxy = uxy && p.d2xxdx2[i] == 0.0;
+    for (int i = 0; i < ny; i++) uxy = uxy && p.d2yydy2[i] == 0.0;
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
@@ -312,9 +460,21 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     c.dxxdx = m; c.d2xxdx2 = m + nx; c.DDX = m + 2 * nx; m += 3 * nx;
     c.dyydy = m; c.d2yydy2 = m + ny; c.DDY = m + 2 * ny; m += 3 * ny;
     c.dzzdz = m; c.d2zzdz2 = m + nz; c.DDZ = m + 2 * nz; c.RKAPA = m + 3 * nz; c.DKAPA = m + 4 * nz; m += 5 * nz;
-    ctx->coef.cx1 = m; ctx->coef.cx2a = m + nx; ctx->coef.cx2b = m + 2 * nx; m += 3 * nx;
-    ctx->coef.cy1 = m; ctx->coef.cy2a = m + ny; ctx->coef.cy2b = m + 2 * ny; m += 3 * ny;
-    ctx->coef.cz1 = m; ctx->coef.cz2a = m + nz; ctx->coef.cz2b = m + 2 * nz;
+    {
+        const double* b0 = ctx->d_metric;
+        const double** c1s[3] = {&ctx->coef.cx1, &ctx->coef.cy1, &ctx->coef.cz1};
+        const double** c2as[3] = {&ctx->coef.cx2a, &ctx->coef.cy2a, &ctx->coef.cz2a};
+        const double** c2bs[3] = {&ctx->coef.cx2b, &ctx->coef.cy2b, &ctx->coef.cz2b};
+        for (int ax = 0; ax < 3; ax++) {
+            *c1s[ax] = b0 + base_off[ax];
+            *c2as[ax] = b0 + base_off[ax] + ns[ax];
+            *c2bs[ax] = b0 + base_off[ax] + 2 * ns[ax];
+            for (int k = 0; k < 6; k++) ctx->coef.s2[ax][k] = b0 + scaled_off[ax] + (size_t)k * ns[ax];
+        }
+        ctx->coef.kapz = b0 + kap_off;
+        ctx->coef.dkapz = b0 + kap_off + nz;
+        ctx->coef.uniform_xy = uxy ? 1 : 0;
+    }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;
     c.GRAV = p.GRAV; c.THETA = p.THETA; c.RE = p.RE; c.REPR = ctx->k.REPR; c.ORE = ctx->k.ORE;
@@ -323,8 +483,19 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     c.izCon = p.izCon; c.iTCon = p.iTCon; c.iBCon = p.iBCon;
 
     ctx->red_blocks = 152 * 8;
-    int arc = alloc_block(ctx, &ctx->U[0], 8);
+    ctx->fp32 = p.precision == MHD_PREC_FP32;
+    ctx->h_cz.assign(h.begin() + base_off[2], h.begin() + base_off[2] + 3 * nz);
+    ctx->h_bg.assign(4 * (size_t)nz, 0.0);
+    int arc = MHD_OK;
+    if (ctx->fp32) {
+        arc = alloc_f32(ctx, &ctx->U32[0]);
+        if (!arc && cudaMalloc(&ctx->d_bg, sizeof(double) * 4 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
+        if (!arc && cudaMemset(ctx->d_bg, 0, sizeof(double) * 4 * nz) != cudaSuccess) arc = MHD_ERR_CUDA;
+    } else {
+        arc = alloc_block(ctx, &ctx->U[0], 8);
+    }
     if (!arc) arc = alloc_block(ctx, &ctx->Zb, 8);
+    if (!arc && ctx->fp32 && (ctx->sw & kSwShr)) arc = alloc_block(ctx, &ctx->FT64, 1);
     if (!arc && cudaMalloc(&ctx->red, sizeof(double) * 8 * (size_t)ctx->red_blocks) != cudaSuccess) arc = MHD_ERR_NOMEM;
     if (!arc && cudaMalloc(&ctx->d_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
     if (!arc && cudaMallocHost(&ctx->h_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
@@ -352,6 +523,10 @@ int mhd_destroy(mhd_ctx* ctx) {
     cudaFree(ctx->Sb);
     cudaFree(ctx->red);
     cudaFree(ctx->d_out);
+    cudaFree(ctx->U32[0]);
+    cudaFree(ctx->U32[1]);
+    cudaFree(ctx->FT64);
+    cudaFree(ctx->d_bg);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -389,6 +564,13 @@ static double* field_ptr(mhd_ctx* ctx, int field, bool for_write, int* rc) {
         if (for_write) ctx->ghosts_synced = false;
         return ctx->U[ctx->cur] + (size_t)field * ctx->ncell;
     }
+    if (ctx->fp32 && field < 16) {
+        if (field != MHD_FT || !ctx->FT64) {
+            *rc = fail(ctx, MHD_ERR_UNSUPPORTED, "an FP32-storage context keeps only FT (with lShr) of the right-hand sides");
+            return nullptr;
+        }
+        return ctx->FT64;
+    }
     if (field < 16) {
         *rc = alloc_block(ctx, &ctx->Fb, 8);
         return *rc ? nullptr : ctx->Fb + (size_t)(field - 8) * ctx->ncell;
@@ -398,6 +580,7 @@ static double* field_ptr(mhd_ctx* ctx, int field, bool for_write, int* rc) {
 
 int mhd_upload(mhd_ctx* ctx, int field, const double* host) {
     if (!ctx || !host) return MHD_ERR_INVALID;
+    if (ctx->fp32 && field >= 0 && field < 8) return upload32(ctx, field, host);
     int rc;
     double* d = field_ptr(ctx, field, true, &rc);
     if (!d) return rc;
@@ -407,6 +590,7 @@ int mhd_upload(mhd_ctx* ctx, int field, const double* host) {
 
 int mhd_download(mhd_ctx* ctx, int field, double* host) {
     if (!ctx || !host) return MHD_ERR_INVALID;
+    if (ctx->fp32 && field >= 0 && field < 8) return download32(ctx, field, host);
     int rc;
     double* d = field_ptr(ctx, field, false, &rc);
     if (!d) return rc;
@@ -417,6 +601,13 @@ int mhd_download(mhd_ctx* ctx, int field, double* host) {
 
 int mhd_upload_state(mhd_ctx* ctx, const double* host) {
     if (!ctx || !host) return MHD_ERR_INVALID;
+    if (ctx->fp32) {
+        for (int f = 0; f < ctx->nf; f++) {
+            int rc = upload32(ctx, f, host + (size_t)f * ctx->ncell);
+            if (rc) return rc;
+        }
+        return MHD_OK;
+    }
     ctx->ghosts_synced = false;
     CK(cudaMemcpyAsync(ctx->U[ctx->cur], host, field_bytes(ctx) * ctx->nf, cudaMemcpyHostToDevice, ctx->stream));
     return MHD_OK;
@@ -424,6 +615,13 @@ int mhd_upload_state(mhd_ctx* ctx, const double* host) {
 
 int mhd_download_state(mhd_ctx* ctx, double* host) {
     if (!ctx || !host) return MHD_ERR_INVALID;
+    if (ctx->fp32) {
+        for (int f = 0; f < ctx->nf; f++) {
+            int rc = download32(ctx, f, host + (size_t)f * ctx->ncell);
+            if (rc) return rc;
+        }
+        return MHD_OK;
+    }
     CK(cudaMemcpyAsync(host, ctx->U[ctx->cur], field_bytes(ctx) * ctx->nf, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return MHD_OK;
@@ -438,6 +636,7 @@ int mhd_set_time(mhd_ctx* ctx, double timt, long long nit) {
 
 int mhd_fluxes(mhd_ctx* ctx) {
     if (!ctx) return MHD_ERR_INVALID;
+    if (ctx->fp32) return fail(ctx, MHD_ERR_UNSUPPORTED, "the unfused calls work on FP64 state only");
     int rc = ensure_parity_buffers(ctx);
     if (rc) return rc;
     double* S = ctx->Sb;
@@ -450,6 +649,7 @@ int mhd_fluxes(mhd_ctx* ctx) {
 
 static int rk(mhd_ctx* ctx, int kind, double coef) {
     if (!ctx) return MHD_ERR_INVALID;
+    if (ctx->fp32) return fail(ctx, MHD_ERR_UNSUPPORTED, "the unfused calls work on FP64 state only");
     int rc = alloc_block(ctx, &ctx->Fb, 8);
     if (rc) return rc;
     if (kind == 2) ctx->ghosts_synced = false;
@@ -465,6 +665,7 @@ int mhd_rk_gam(mhd_ctx* ctx, double coef) { return rk(ctx, 2, coef); }
 
 int mhd_bcon(mhd_ctx* ctx, double timt) {
     if (!ctx) return MHD_ERR_INVALID;
+    if (ctx->fp32) return fail(ctx, MHD_ERR_UNSUPPORTED, "the unfused calls work on FP64 state only");
     const int e = parity_bcon(ctx->sw, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), timt, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "BCON launch");
     return MHD_OK;
@@ -473,6 +674,11 @@ int mhd_bcon(mhd_ctx* ctx, double timt) {
 int mhd_communicate(mhd_ctx* ctx) {
     if (!ctx) return MHD_ERR_INVALID;
     ctx->ghosts_synced = false;
+    if (ctx->fp32) {
+        const int e = communicate32(ctx->nf, ctx->g, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "communicate launch");
+        return MHD_OK;
+    }
     const int e = parity_communicate(ctx->nf, ctx->g, fields_of(ctx, ctx->U[ctx->cur]), ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "communicate launch");
     return MHD_OK;
@@ -481,8 +687,11 @@ int mhd_communicate(mhd_ctx* ctx) {
 int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach) {
     if (!ctx) return MHD_ERR_INVALID;
     const bool mag = (ctx->sw & kSwMag) != 0;
-    int e = parity_cfl(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks, ctx->d_out,
-                       ctx->stream);
+    const int nz = ctx->g.nz;
+    int e = ctx->fp32 ? cfl32(mag, ctx->g, ctx->c, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->d_bg, ctx->d_bg + nz,
+                              ctx->red, ctx->red_blocks, ctx->d_out, ctx->stream)
+                      : parity_cfl(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks,
+                                   ctx->d_out, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "CFL launch");
     CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -520,7 +729,7 @@ int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out) {
         if (rc) return rc;
         if (dt < 1.0e-8f) return fail(ctx, MHD_ERR_DT_TOO_SMALL, "DT too small, halt (3dmhd.cpp:292-331)");
     }
-    rc = ctx->prm.path == MHD_PATH_PARITY ? parity_step(ctx, dt) : fused_step(ctx, dt);
+    rc = ctx->fp32 ? fused32_step(ctx, dt) : ctx->prm.path == MHD_PATH_PARITY ? parity_step(ctx, dt) : fused_step(ctx, dt);
     if (rc) return rc;
     // 3dmhdsub.h:150-152 (TIMI + TIMC accumulates the same way)
     ctx->nit += 1;
@@ -548,8 +757,11 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt) {
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out) {
     if (!ctx || !out) return MHD_ERR_INVALID;
     const bool mag = (ctx->sw & kSwMag) != 0;
-    int e = diag_reduce(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks, ctx->d_out,
-                        ctx->stream);
+    const int nz = ctx->g.nz;
+    int e = ctx->fp32 ? diag32(mag, ctx->g, ctx->c, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->d_bg, ctx->d_bg + nz,
+                               ctx->red, ctx->red_blocks, ctx->d_out, ctx->stream)
+                      : diag_reduce(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks,
+                                    ctx->d_out, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "diagnostics launch");
     CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(double) * 4, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -60,6 +60,11 @@ struct Coefs {
     const double *cx1, *cx2a, *cx2b;
     const double *cy1, *cy2a, *cy2b;
     const double *cz1, *cz2a, *cz2b;
+    // second-derivative coefficients with the viscous and resistive scales
+    // folded in, per axis: ORE*c2a, ORE*c2b, ORE*C43*c2a, ORE*C43*c2b, ORM*c2a, ORM*c2b
+    const double* s2[3][6];
+    const double *kapz, *dkapz;  // (OCV/REPR)*RKAPA[z], (OCV/REPR)*DKAPA[z]
+    int uniform_xy;              // d2xxdx2 and d2yydy2 vanish everywhere
 };
 
 // ---- launchers implemented in the .cu files ----------------------------
@@ -94,10 +99,51 @@ struct FusedArgs {
     double* FT;    // persistent temperature right-hand side (lShr only)
     double gdt;    // GAM_k * dt
     double zdt;    // ZETA_k * dt
+    double timt;   // simulation time seen by BCON
     int substage;  // 0, 1, 2
 };
 int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st);
+// Ragged batches: persistent CTAs take (instance, tile x, tile y) items from a
+// counter that must be zero at launch.  Tile shapes: 0 = 32x4, 1 = 32x8, 2 = 16x8.
+constexpr int kBatchTiles = 3;
+void batch_tile_dims(int tile, int* tx, int* ty);
+// _uxy: uniform x/y grids (d2xxdx2 = d2yydy2 = 0); _gen: any grid.
+// Item w = first z plane | (end plane << 16).
+int fused_batch_substage_uxy(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
+                             int grid, cudaStream_t st);
+int fused_batch_substage_gen(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
+                             int grid, cudaStream_t st);
+int fused_batch_occupancy_uxy(unsigned sw, int tile, int* blocks_per_sm);
+int fused_batch_occupancy_gen(unsigned sw, int tile, int* blocks_per_sm);
+int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, int nblocks, cudaStream_t st);
 int fused_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
+
+// FP32-storage path (fields stored in FP32, RO and TT as deviations from FP64
+// reference profiles rho0(z), T0(z)).
+struct Fields8f {
+    float* p[8];
+};
+struct Fused32Args {
+    Grid g;
+    Consts c;
+    Coefs k;
+    Fields8f U;    // state read (deviation form, with ghosts)
+    Fields8f Uo;   // state written
+    Fields8 Z;     // FP64 RK register (full values)
+    double* FT;    // FP64 persistent temperature right-hand side (lShr only)
+    const double *bgR, *bgT;     // reference profiles rho0(z), T0(z)
+    const double *dzT0, *d2zT0;  // their premultiplied first and second z derivatives
+    double gdt, zdt;
+    int substage;
+};
+int fused32_substage(unsigned sw, const Fused32Args& a, cudaStream_t st);
+int fused32_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const double* bgR,
+                       const double* bgT, double timt, cudaStream_t st);
+int communicate32(int nf, const Grid& g, Fields8f U, cudaStream_t st);
+int cfl32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT, double* partials,
+          int max_blocks, double* out5, cudaStream_t st);
+int diag32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
+           double* partials, int max_blocks, double* out4, cudaStream_t st);
 
 constexpr unsigned kSwRot = 0x1u, kSwMag = 0x2u, kSwShr = 0x10u;
 

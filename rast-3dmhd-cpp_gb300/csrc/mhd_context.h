@@ -1,0 +1,58 @@
+// mhd_context.h -- the context behind mhd_ctx* (private to the library).
+#pragma once
+
+#include "../../include/mhd_gb300.h"
+#include "mhd_common.cuh"
+
+#include <string>
+#include <vector>
+
+using namespace mhd;
+
+struct mhd_ctx {
+    mhd_params prm{};
+    mhd_constants k{};
+    Grid g{};
+    Consts c{};
+    Coefs coef{};
+    unsigned sw = 0;
+    int nf = 5;
+    size_t ncell = 0;  // nx*ny*nz
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double* d_metric = nullptr;  // 11 metric arrays + 9 coefficient arrays
+    double* U[2] = {nullptr, nullptr};
+    int cur = 0;
+    double* Zb = nullptr;
+    double* Fb = nullptr;
+    double* Sb = nullptr;
+    double* red = nullptr;   // reduction partials
+    double* d_out = nullptr; // 8 doubles of reduction results
+    double* h_out = nullptr; // pinned mirror of d_out
+    int red_blocks = 0;
+    bool ghosts_synced = false;  // z ghost planes of U[1-cur] match U[cur]
+    double timt = 0.0;
+    long long nit = 0;
+    double last_dt = 0.0, last_umach = 0.0;
+    size_t bytes = 0;
+    std::string err;
+    // FP32-storage contexts
+    bool fp32 = false;
+    float* U32[2] = {nullptr, nullptr};
+    double* FT64 = nullptr;     // persistent FT (lShr)
+    double* d_bg = nullptr;     // rho0, T0, dzT0, d2zT0 (4 x nz)
+    std::vector<double> h_bg;   // host copy of the four profiles
+    std::vector<double> h_cz;   // cz1, cz2a, cz2b (3 x nz)
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;  // pairs around each substage launch
+    size_t prof_used = 0;
+};
+
+namespace mhd::ctxops {
+int ensure_u1(mhd_ctx* ctx);
+int sync_zghosts(mhd_ctx* ctx);
+int alloc_block(mhd_ctx* ctx, double** p, int nfields);
+Fields8 fields_of(const mhd_ctx* c, double* base);
+int fail(mhd_ctx* c, int code, const std::string& msg);
+}  // namespace mhd::ctxops

@@ -1,0 +1,392 @@
+// mhd_fused_tile.cuh -- the fused FP64 RK3 substage for one tile of columns.
+//
+// A CTA owns a TX x TY tile of (x, y) columns and marches down a range of z
+// planes.  Three z-planes of the tile plus a one-cell halo live in a
+// shared-memory ring; when plane z+2 is loaded its derived quantities (1/rho,
+// the velocities u = RU/rho, v, w and the pressure p = rho*T) are computed
+// once per point, so every stencil reads them instead of recomputing them.
+// One thread per column then evaluates the whole right-hand side of fluxes()
+// (3dmhdsub.h:194-696) for cell (z, y, x), applies the RK update of
+// step_block_GAM (3dmhdsub.h:181-192), forms the next substage's register
+// Z' = U' + zeta*dt*F (step_block_ZETA, 3dmhdsub.h:168-179) and writes U'
+// together with its periodic ghost images (communicate(), 3dmhdmpi.h:11-143,
+// as dual stores).  BCON (3dmhdsub.h:720-873) on the wall planes follows in a
+// separate small kernel.
+//
+// GB300 executes two FP64 FMAs per clock per SM, so this kernel is bound by
+// its FP64 instruction count, not by HBM; the right-hand side is regrouped for
+// the fewest FP64 instructions:
+//   * metric factors are premultiplied (c1 = duudu*hu, c2a = d2uudu2*hu,
+//     c2b = duudu^2*h2u), and the viscous (ORE, ORE*C43) and resistive (ORM)
+//     scales are folded into copies of c2a/c2b, so a scaled second derivative
+//     accumulates with three FMAs (five where d2uudu2 does not vanish);
+//   * UXY (uniform x and y grids, d2uudu2 = 0) drops the first-derivative
+//     part of the x/y second derivatives at compile time;
+//   * repeated gradients are computed once; 1/rho is Newton's iteration
+//     r <- r + r(1 - rho r), twice, from the hardware reciprocal estimate.
+// Results agree with the reference to rounding (1e-12 of each field's
+// max-norm after a step, checked against the oracle).
+//
+// Wall planes: the values the reference overwrites in BCON (RU, RV, RW, TT,
+// BZ and, with lShr, the right-hand side FT) are finite but not the
+// reference's before BCON runs; RO, BX, BY and everything on interior planes
+// follow the reference.  The z ghost planes are never written (the reference
+// only flips RO there between rho and 1/rho; those values reach no result).
+#pragma once
+
+#include "mhd_common.cuh"
+
+namespace mhd {
+namespace fused {
+
+template <int TX, int TY>
+struct Tile {
+    static constexpr int kTX = TX;
+    static constexpr int kTY = TY;
+    static constexpr int kThreads = TX * TY;
+    static constexpr int kPX = TX + 2;
+    static constexpr int kPY = TY + 2;
+    static constexpr int kPlane = kPX * kPY;
+};
+
+// quantities held per plane point
+enum Q { Q_RU = 0, Q_RV, Q_RW, Q_TT, Q_RO, Q_RI, Q_U, Q_V, Q_W, Q_P, Q_BX, Q_BY, Q_BZ, Q_N };
+
+template <class SW>
+constexpr int nq() {
+    return SW::lMag ? Q_N : Q_BX;
+}
+
+template <class SW, class T>
+constexpr size_t ring_bytes() {
+    return (size_t)3 * nq<SW>() * T::kPlane * sizeof(double);
+}
+
+// 1/x by Newton's iteration for the reciprocal, r <- r + r(1 - x r), applied
+// twice to the hardware estimate (each step doubles the correct bits).
+__device__ __forceinline__ double recip(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+template <class SW, class T>
+__device__ __forceinline__ void load_plane(const FusedArgs& a, double* ring, int slot, int z, int x0, int y0) {
+    constexpr int NQ = nq<SW>();
+    constexpr int kPlane = T::kPlane, kPX = T::kPX, kThreads = T::kThreads;
+    double* base = ring + (size_t)slot * NQ * kPlane;
+    const Grid& g = a.g;
+    for (int k = threadIdx.x; k < kPlane; k += kThreads) {
+        const int hx = k % kPX, hy = k / kPX;
+        const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+        if (gx >= g.nx || gy >= g.ny) continue;
+        const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
+        const double ru = a.U.p[S_RU][i], rv = a.U.p[S_RV][i], rw = a.U.p[S_RW][i];
+        const double tt = a.U.p[S_TT][i], ro = a.U.p[S_RO][i];
+        const double ri = recip(ro);
+        base[Q_RU * kPlane + k] = ru;
+        base[Q_RV * kPlane + k] = rv;
+        base[Q_RW * kPlane + k] = rw;
+        base[Q_TT * kPlane + k] = tt;
+        base[Q_RO * kPlane + k] = ro;
+        base[Q_RI * kPlane + k] = ri;
+        base[Q_U * kPlane + k] = ru * ri;
+        base[Q_V * kPlane + k] = rv * ri;
+        base[Q_W * kPlane + k] = rw * ri;
+        base[Q_P * kPlane + k] = ro * tt;
+        if constexpr (SW::lMag) {
+            base[Q_BX * kPlane + k] = a.U.p[S_BX][i];
+            base[Q_BY * kPlane + k] = a.U.p[S_BY][i];
+            base[Q_BZ * kPlane + k] = a.U.p[S_BZ][i];
+        }
+    }
+}
+
+// Store v at (z, y, x) and at every periodic ghost image of that cell.
+__device__ __forceinline__ void store_with_images(double* F, const Grid& g, int z, int y, int x, double v) {
+    const long long zo = (long long)z * g.sz;
+    const int yb = (y == 1) ? g.ny - 1 : (y == g.ny - 2 ? 0 : -1);
+    const int xb = (x == 1) ? g.nx - 1 : (x == g.nx - 2 ? 0 : -1);
+    F[zo + (long long)y * g.sy + x] = v;
+    if (xb >= 0) F[zo + (long long)y * g.sy + xb] = v;
+    if (yb >= 0) {
+        F[zo + (long long)yb * g.sy + x] = v;
+        if (xb >= 0) F[zo + (long long)yb * g.sy + xb] = v;
+    }
+}
+
+// acc + s * D2 F at a node from F[+1], F[-1], F[0], with s folded into
+// (c2a_s, c2b_s); HAS_A = false when d2uudu2 vanishes on this axis.
+template <bool HAS_A>
+__device__ __forceinline__ double acc_d2(double acc, double p, double m, double c, double c2a_s, double c2b_s) {
+    acc = fma(fma(-2.0, c, p + m), c2b_s, acc);
+    if constexpr (HAS_A) acc = fma(p - m, c2a_s, acc);
+    return acc;
+}
+
+// One tile (bx, by) of one instance, z planes [zb, ze) of the interior.
+template <class SW, class T, bool UXY>
+__device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by, int zb, int ze, double* ring) {
+    constexpr int NQ = nq<SW>();
+    constexpr int kTX = T::kTX, kPX = T::kPX, kPlane = T::kPlane, kTY = T::kTY;
+    const Grid& g = a.g;
+    const Consts& c = a.c;
+    const Coefs& K = a.k;
+    const int x0 = 1 + bx * kTX, y0 = 1 + by * kTY;
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool active = (x <= g.nx - 2) && (y <= g.ny - 2);
+    const int zl = 1, zr = g.nz - 1;
+
+    // per-column coefficients
+    const int xc = active ? x : 1, yc = active ? y : 1;
+    const double cx1 = K.cx1[xc], cy1 = K.cy1[yc];
+    const double cx2a = K.cx2a[xc], cx2b = K.cx2b[xc], cy2a = K.cy2a[yc], cy2b = K.cy2b[yc];
+    // folded viscous / resistive coefficients: [ORE a, ORE b, ORE43 a, ORE43 b, ORM a, ORM b]
+    double sx[6], sy[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        sx[k] = K.s2[0][k][xc];
+        sy[k] = K.s2[1][k][yc];
+    }
+    const double c13ore = c.C13 * c.ORE;
+    const double kxy = c13ore * cx1 * cy1;
+    const double kx13 = c13ore * cx1, ky13 = c13ore * cy1;
+    const double ocvore = c.OCV * c.ORE;
+    const double ohm = c.OBETA * c.ORM * c.OCV;
+
+    load_plane<SW, T>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
+    load_plane<SW, T>(a, ring, zb % 3, zb, x0, y0);
+    load_plane<SW, T>(a, ring, (zb + 1) % 3, zb + 1, x0, y0);
+
+    const int pc = (ty + 1) * kPX + (tx + 1);  // centre offset inside a plane
+    for (int z = zb; z < ze; z++) {
+        __syncthreads();
+        if (active) {
+            const double* Pm = ring + (size_t)((z - 1) % 3) * NQ * kPlane;
+            const double* P0 = ring + (size_t)(z % 3) * NQ * kPlane;
+            const double* Pp = ring + (size_t)((z + 1) % 3) * NQ * kPlane;
+            auto C0 = [&](int q) { return P0[q * kPlane + pc]; };
+            auto XP = [&](int q) { return P0[q * kPlane + pc + 1]; };
+            auto XM = [&](int q) { return P0[q * kPlane + pc - 1]; };
+            auto YP = [&](int q) { return P0[q * kPlane + pc + kPX]; };
+            auto YM = [&](int q) { return P0[q * kPlane + pc - kPX]; };
+            auto ZP = [&](int q) { return Pp[q * kPlane + pc]; };
+            auto ZM = [&](int q) { return Pm[q * kPlane + pc]; };
+            const double cz1 = K.cz1[z], cz2a = K.cz2a[z], cz2b = K.cz2b[z];
+            double sz[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) sz[k] = K.s2[2][k][z];
+            auto Dx = [&](int q) { return (XP(q) - XM(q)) * cx1; };
+            auto Dy = [&](int q) { return (YP(q) - YM(q)) * cy1; };
+            auto Dz = [&](int q) { return (ZP(q) - ZM(q)) * cz1; };
+            // acc + s * (D2x + D2y + D2z) q with scale pair k (0: ORE, 1: ORE*C43, 2: ORM)
+            auto lapx = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, XP(q), XM(q), C0(q), sx[2 * k], sx[2 * k + 1]); };
+            auto lapy = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, YP(q), YM(q), C0(q), sy[2 * k], sy[2 * k + 1]); };
+            auto lapz = [&](double acc, int q, int k) { return acc_d2<true>(acc, ZP(q), ZM(q), C0(q), sz[2 * k], sz[2 * k + 1]); };
+
+            const double ro = C0(Q_RO), ri = C0(Q_RI), tt = C0(Q_TT);
+            const double u = C0(Q_U), v = C0(Q_V), w = C0(Q_W);
+            const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
+
+            // ---- continuity (3dmhdsub.h:204-227), one-sided dRW/dz on the walls
+            double rwz = ZP(Q_RW) - ZM(Q_RW);
+            if (z == zl) rwz = 4.0 * ZP(Q_RW) - a.U.p[S_RW][i + 2 * g.sz];
+            if (z == zr - 1) rwz = a.U.p[S_RW][i - 2 * g.sz] - 4.0 * ZM(Q_RW);
+            const double fr = -fma(rwz, cz1, fma(YP(Q_RV) - YM(Q_RV), cy1, (XP(Q_RU) - XM(Q_RU)) * cx1));
+
+            // ---- pressure and gravity (3dmhdsub.h:266-272)
+            double fu = -Dx(Q_P);
+            double fv = -Dy(Q_P);
+            double fw = fma(ro, c.GRAV, -Dz(Q_P));
+
+            // ---- momentum advection (3dmhdsub.h:279-289): -D_j(RU_i u_j)
+            fu = fma(-cx1, fma(XP(Q_RU), XP(Q_U), -XM(Q_RU) * XM(Q_U)), fu);
+            fu = fma(-cy1, fma(YP(Q_RU), YP(Q_V), -YM(Q_RU) * YM(Q_V)), fu);
+            fu = fma(-cz1, fma(ZP(Q_RU), ZP(Q_W), -ZM(Q_RU) * ZM(Q_W)), fu);
+            fv = fma(-cx1, fma(XP(Q_RV), XP(Q_U), -XM(Q_RV) * XM(Q_U)), fv);
+            fv = fma(-cy1, fma(YP(Q_RV), YP(Q_V), -YM(Q_RV) * YM(Q_V)), fv);
+            fv = fma(-cz1, fma(ZP(Q_RV), ZP(Q_W), -ZM(Q_RV) * ZM(Q_W)), fv);
+            fw = fma(-cx1, fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U)), fw);
+            fw = fma(-cy1, fma(YP(Q_RW), YP(Q_V), -YM(Q_RW) * YM(Q_V)), fw);
+            fw = fma(-cz1, fma(ZP(Q_RW), ZP(Q_W), -ZM(Q_RW) * ZM(Q_W)), fw);
+
+            // ---- temperature: advection (3dmhdsub.h:293-296), conduction (:315-319)
+            const double Tz = Dz(Q_TT);
+            double ft;
+            if constexpr (!SW::lShr) {
+                ft = -fma(u, Dx(Q_TT), fma(v, Dy(Q_TT), w * Tz));
+            } else {
+                ft = a.FT[i];  // the reference never re-initialises FT with lShr
+            }
+            {
+                double lapT = acc_d2<!UXY>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
+                lapT = acc_d2<!UXY>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
+                lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
+                ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+            }
+
+            // ---- viscous Laplacians (3dmhdsub.h:462-472)
+            fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
+            fv = lapz(lapy(lapx(fv, Q_V, 0), Q_V, 1), Q_V, 0);
+            fw = lapz(lapy(lapx(fw, Q_W, 0), Q_W, 0), Q_W, 1);
+
+            // ---- viscous cross terms (3dmhdsub.h:486-487,517-518,531-532)
+            {
+                const double kxz = kx13 * cz1, kyz = ky13 * cz1;
+                auto E = [&](const double* Pl, int q, int off) { return Pl[q * kPlane + pc + off]; };
+                const double dyxv = (E(P0, Q_V, kPX + 1) - E(P0, Q_V, kPX - 1)) - (E(P0, Q_V, -kPX + 1) - E(P0, Q_V, -kPX - 1));
+                const double dyxu = (E(P0, Q_U, kPX + 1) - E(P0, Q_U, kPX - 1)) - (E(P0, Q_U, -kPX + 1) - E(P0, Q_U, -kPX - 1));
+                const double dxzw = (E(Pp, Q_W, 1) - E(Pm, Q_W, 1)) - (E(Pp, Q_W, -1) - E(Pm, Q_W, -1));
+                const double dyzw = (E(Pp, Q_W, kPX) - E(Pm, Q_W, kPX)) - (E(Pp, Q_W, -kPX) - E(Pm, Q_W, -kPX));
+                const double dxzu = (E(Pp, Q_U, 1) - E(Pm, Q_U, 1)) - (E(Pp, Q_U, -1) - E(Pm, Q_U, -1));
+                const double dyzv = (E(Pp, Q_V, kPX) - E(Pm, Q_V, kPX)) - (E(Pp, Q_V, -kPX) - E(Pm, Q_V, -kPX));
+                fu = fma(kxy, dyxv, fma(kxz, dxzw, fu));
+                fv = fma(kxy, dyxu, fma(kyz, dyzw, fv));
+                fw = fma(kxz, dxzu, fma(kyz, dyzv, fw));
+            }
+
+            // velocity gradients (heating and induction)
+            double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
+            if constexpr (!SW::lShr || SW::lMag) {
+                ux = Dx(Q_U); uy = Dy(Q_U); uz = Dz(Q_U);
+                vx = Dx(Q_V); vy = Dy(Q_V); vz = Dz(Q_V);
+                wx = Dx(Q_W); wy = Dy(Q_W); wz = Dz(Q_W);
+            }
+            // ---- viscous heating and pdV work (3dmhdsub.h:477-538, not with lShr)
+            if constexpr (!SW::lShr) {
+                double dg = ux * ux;
+                dg = fma(vy, vy, dg);
+                dg = fma(wz, wz, dg);
+                dg = fma(-ux, vy, dg);
+                dg = fma(-ux, wz, dg);
+                dg = fma(-vy, wz, dg);
+                const double s1 = uy + vx, s2 = uz + wx, s3 = vz + wy;
+                const double sh = fma(s1, s1, fma(s2, s2, s3 * s3));
+                const double phi = fma(c.C43, dg, sh);
+                ft = fma(ocvore * ri, phi, ft);
+                ft = fma(-c.OCV * tt, ux + vy + wz, ft);
+            }
+
+            // ---- Coriolis (3dmhdsub.h:540-545)
+            if constexpr (SW::lRot) {
+                fu = fma(c.OMZ, C0(Q_RV), fu);
+                fv = fma(-c.OMZ, C0(Q_RU), fv);
+                fv = fma(c.OMX, C0(Q_RW), fv);
+                fw = fma(-c.OMX, C0(Q_RV), fw);
+            }
+
+            // ---- induction, Lorentz force, Ohmic heating (3dmhdsub.h:547-695)
+            double w1 = 0, w2 = 0, w3 = 0;
+            if constexpr (SW::lMag) {
+                const double bx = C0(Q_BX), by = C0(Q_BY), bz = C0(Q_BZ);
+                // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
+                double wzm = wz;
+                if (z == zl) {
+                    const long long j = i + 2 * g.sz;
+                    wzm = (4.0 * ZP(Q_W) - a.U.p[S_RW][j] / a.U.p[S_RO][j]) * cz1;
+                }
+                if (z == zr - 1) {
+                    const long long j = i - 2 * g.sz;
+                    wzm = (a.U.p[S_RW][j] / a.U.p[S_RO][j] - 4.0 * ZM(Q_W)) * cz1;
+                }
+                const double bxx = Dx(Q_BX), bxy = Dy(Q_BX), bxz = Dz(Q_BX);
+                const double byx = Dx(Q_BY), byy = Dy(Q_BY), byz = Dz(Q_BY);
+                const double bzx = Dx(Q_BZ), bzy = Dy(Q_BZ), bzz = Dz(Q_BZ);
+                w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
+                w1 = fma(-u, bxx, fma(-v, bxy, fma(-w, bxz, w1)));
+                w1 = lapy(lapx(w1, Q_BX, 2), Q_BX, 2);
+                w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
+                w2 = fma(-u, byx, fma(-v, byy, fma(-w, byz, w2)));
+                w2 = lapy(lapx(w2, Q_BY, 2), Q_BY, 2);
+                w3 = fma(bx, wx, fma(by, wy, -bz * (ux + vy)));
+                w3 = fma(-u, bzx, fma(-v, bzy, fma(-w, bzz, w3)));
+                w3 = lapz(lapy(lapx(w3, Q_BZ, 2), Q_BZ, 2), Q_BZ, 2);
+                // d2B/dz2 with the one-sided wall stencils (3dmhdsub.h:640-654,673-687)
+                if (z == zl || z == zr - 1) {
+                    const int s = (z == zl) ? 1 : -1;
+                    const long long j2 = i + 2 * s * g.sz, j3 = i + 3 * s * g.sz;
+                    const double d2 = c.d2zzdz2[z] * c.hz * c.ORM, d1 = c.dzzdz[z] * c.dzzdz[z] * c.h2z * c.ORM;
+                    const double X1 = (s > 0) ? ZP(Q_BX) : ZM(Q_BX), X2 = a.U.p[S_BX][j2], X3 = a.U.p[S_BX][j3];
+                    const double Y1 = (s > 0) ? ZP(Q_BY) : ZM(Q_BY), Y2 = a.U.p[S_BY][j2], Y3 = a.U.p[S_BY][j3];
+                    const double sg = (double)s;
+                    w1 += sg * (-3.0 * bx + 4.0 * X1 - X2) * d2 + (2.0 * bx - 5.0 * X1 + 4.0 * X2 - X3) * d1;
+                    w2 += sg * (-3.0 * by + 4.0 * Y1 - Y2) * d2 + (2.0 * by - 5.0 * Y1 + 4.0 * Y2 - Y3) * d1;
+                } else {
+                    w1 = lapz(w1, Q_BX, 2);
+                    w2 = lapz(w2, Q_BY, 2);
+                }
+                const double jz = byx - bxy, jy = bxz - bzx, jx = bzy - byz;
+                fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
+                fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
+                fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
+                ft = fma(ohm * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+            }
+
+            // ---- RK3 substage update and the next register (3dmhdsub.h:168-192)
+            const double fl[8] = {fu, fv, fw, ft, fr, w1, w2, w3};
+            constexpr int nf = SW::lMag ? 8 : 5;
+            constexpr int ring_of[8] = {Q_RU, Q_RV, Q_RW, Q_TT, Q_RO, Q_BX, Q_BY, Q_BZ};
+#pragma unroll
+            for (int f = 0; f < nf; f++) {
+                const double zf = (a.substage == 0) ? C0(ring_of[f]) : a.Z.p[f][i];
+                const double un = fma(a.gdt, fl[f], zf);
+                store_with_images(a.Uo.p[f], g, z, y, x, un);
+                if (a.substage < 2) a.Z.p[f][i] = fma(a.zdt, fl[f], un);
+            }
+            if constexpr (SW::lShr) a.FT[i] = ft;
+        }
+        __syncthreads();
+        if (z + 2 <= ze) load_plane<SW, T>(a, ring, (z + 2) % 3, z + 2, x0, y0);
+    }
+}
+
+// BCON (3dmhdsub.h:720-873) for one wall cell of U' plus its periodic ghost images.
+template <class SW>
+__device__ __forceinline__ void bcon_cell(const Grid& g, const Consts& c, const Fields8& U, double timt, int wall, int x,
+                                          int y) {
+    const long long sz = g.sz;
+    const double RRT = 1.0, RRB = -1.0, RPP = 0.0;
+    const int z = wall == 0 ? 1 : g.nz - 2;
+    const int s = wall == 0 ? 1 : -1;
+    const long long i = (long long)z * sz + (long long)y * g.sy + x;
+    const long long i1 = i + s * sz, i2 = i + 2 * s * sz;
+    const double *RU = U.p[S_RU], *RV = U.p[S_RV], *TT = U.p[S_TT], *RO = U.p[S_RO];
+    double ru, rv, tt;
+    if constexpr (SW::lShr) {
+        ru = 0.0;
+        rv = (wall == 0 ? RRT : RRB) * cos(RPP * timt) * RO[i];
+    } else {
+        ru = RO[i] * (c.C43 * RU[i1] / RO[i1] - c.C13 * RU[i2] / RO[i2]);
+        rv = RO[i] * (c.C43 * RV[i1] / RO[i1] - c.C13 * RV[i2] / RO[i2]);
+    }
+    if (wall == 0) {
+        if (c.iTCon == 1) {
+            const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
+            tt = c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA;
+        } else {
+            tt = 1.0;
+            if (c.iTCon == 4 && x < g.nx / 2) tt = 1.0f - c.TP;
+        }
+    } else {
+        if (c.izCon == 0) {
+            tt = c.TB;
+        } else {
+            const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
+            tt = c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA / c.RKAPA[z];
+        }
+    }
+    store_with_images(U.p[S_RU], g, z, y, x, ru);
+    store_with_images(U.p[S_RV], g, z, y, x, rv);
+    store_with_images(U.p[S_RW], g, z, y, x, 0.0);
+    store_with_images(U.p[S_TT], g, z, y, x, tt);
+    if constexpr (SW::lMag) {
+        if (c.iBCon == 0) store_with_images(U.p[S_BZ], g, z, y, x, 0.0);
+    }
+}
+
+}  // namespace fused
+}  // namespace mhd

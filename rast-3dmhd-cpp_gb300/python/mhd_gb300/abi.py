@@ -90,6 +90,7 @@ SIGNATURES = {
     "mhd_upload_state": [C.c_void_p, _DP],
     "mhd_download_state": [C.c_void_p, _DP],
     "mhd_set_time": [C.c_void_p, C.c_double, C.c_longlong],
+    "mhd_init_polytrope": [C.c_void_p, _DP, C.c_double, C.c_ulonglong, C.c_double],
     "mhd_fluxes": [C.c_void_p],
     "mhd_rk_zeta0": [C.c_void_p],
     "mhd_rk_zeta": [C.c_void_p, C.c_double],
@@ -101,6 +102,15 @@ SIGNATURES = {
     "mhd_steps": [C.c_void_p, C.c_int, C.c_double],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],
+    "mhd_batch_create": [C.POINTER(C.c_void_p), _DP, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)],
+    "mhd_batch_destroy": [C.c_void_p],
+    "mhd_batch_set_tile": [C.c_void_p, C.c_int],
+    "mhd_batch_tile": [C.c_void_p, C.POINTER(C.c_int)],
+    "mhd_batch_autotune": [C.c_void_p, C.POINTER(C.c_int), _DP],
+    "mhd_batch_steps": [C.c_void_p, C.c_int],
+    "mhd_batch_sync": [C.c_void_p],
+    "mhd_write_dat0": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_int],
+    "mhd_read_dat0": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_int],
     "mhd_set_device": [C.c_int],
     "mhd_timer_start": [C.c_void_p],
     "mhd_timer_stop": [C.c_void_p, _DP],

@@ -227,6 +227,48 @@ def initial_state(case: Case) -> dict[str, np.ndarray]:
     return st
 
 
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
+def device_initial_state(case: Case) -> dict[str, np.ndarray]:
+    """Host mirror of the device initial state (mhd_init_polytrope): the same
+    polytrope as initial_state, with the Gaussian noise drawn by Box-Muller
+    from splitmix64 of (seed, interior cell index) instead of numpy's stream."""
+    nz, ny, nx = case.shape
+    z = z_coordinate(case)
+    m = case.GRAV / case.THETA - 1.0
+    T1 = 1.0 + case.THETA * z
+    R1 = T1 ** m
+    cell = np.arange(case.nPz * case.nPy * case.nPx, dtype=np.uint64)
+    seed = np.uint64(int(case.seed) & 0xFFFFFFFFFFFFFFFF)
+    h1 = _splitmix64(seed ^ _splitmix64(np.uint64(2) * cell))
+    h2 = _splitmix64(seed ^ _splitmix64(np.uint64(2) * cell + np.uint64(1)))
+    u1 = ((h1 >> np.uint64(11)) + np.uint64(1)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    u2 = ((h2 >> np.uint64(11)) + np.uint64(1)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    gauss = (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)).reshape(case.nPz, case.nPy, case.nPx)
+    TT = np.broadcast_to(T1[:, None, None], case.shape).copy()
+    RO = np.broadcast_to(R1[:, None, None], case.shape).copy()
+    TT[1:-1, 1:-1, 1:-1] *= 1.0 + case.noise * gauss
+    st = {k: np.zeros(case.shape) for k in STATE_FIELDS}
+    st["TT"], st["RO"] = TT, RO
+    if case.lMag:
+        st["BZ"][2:-2, :, :] = case.bz0
+    if case.lShr:
+        st["RV"][1] = RO[1]
+        st["RV"][-2] = -RO[-2]
+    for k in STATE_FIELDS:
+        periodic_fill(st[k])
+    return st
+
+
 def small_cases() -> dict[str, Case]:
     """Small switch-coverage cases shared by the golden fixtures and the
     parity tests (grid sizes the CPU oracle finishes in well under a second)."""
@@ -245,6 +287,28 @@ def config0() -> Case:
     density contrast 10), tanh z grid (1.5), noise 1e-3, Bz=1e-3, 1/Re=1e-2,
     Pr=1, Pm=1, dt=1e-4, 100 steps; the oracle runs it on 2x2 ranks."""
     return Case(name="config0_64x64x32", nPx=64, nPy=64, nPz=32, lMag=True, seed=1, nPEy=2, nPEz=2)
+
+
+def config3() -> Case:
+    """256x256x128 MHD seeded as the plain-method configuration but with
+    noise amplitude 1e-2: the FP32-storage precision run (1000 steps)."""
+    return Case(name="config3_256x256x128", nPx=256, nPy=256, nPz=128, lMag=True, noise=1e-2, seed=1, nPEy=2, nPEz=2)
+
+
+def config2_batch(n: int = 64, seed: int = 2) -> list:
+    """64 independent FP64 MHD instances of uneven sizes: nx = ny from
+    {32, 48, 64, 96, 128}, nz from {32, 64}, per-instance seed, 1/Re
+    log-uniform in [3e-3, 3e-2], Bz0 log-uniform in [1e-4, 1e-2]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nxy = int(rng.choice([32, 48, 64, 96, 128]))
+        nz = int(rng.choice([32, 64]))
+        ore = float(np.exp(rng.uniform(np.log(3e-3), np.log(3e-2))))
+        bz = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-2))))
+        out.append(Case(name=f"batch{i}", nPx=nxy, nPy=nxy, nPz=nz, lMag=True, RE=1.0 / ore, bz0=bz,
+                        seed=int(rng.integers(1 << 30))))
+    return out
 
 
 def config1() -> Case:

@@ -1,0 +1,253 @@
+"""Continuous-batching server for independent 3dmhd simulations on one GPU.
+
+Requests (a grid, a step count, a precision, a seed) arrive over time.  The
+server admits a waiting request as soon as its device memory fits in the HBM
+budget next to the simulations already resident, uploads its initial state,
+and steps every resident simulation together: FP64 simulations with the same
+switch set form one ragged batch (one persistent launch per RK3 substage over
+all of their tiles, each step a CUDA graph), FP32-storage simulations run on
+their own streams, so their kernels overlap with the batch.  A simulation
+leaves when its step count is reached; its memory is freed at once and the
+next waiting request takes the slot.  Each step of each simulation computes
+exactly what it would compute alone (the per-cell arithmetic does not depend
+on the mix), so results are the same alone and in the mix.
+
+Time-to-solution of a request = completion time - arrival time; the server
+reports p50 / p99 of it and the aggregate cell-RK3-updates/s.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .case import Case, STATE_FIELDS, device_initial_state, initial_state
+from .sim import Batch, Simulation
+
+
+@dataclass
+class Request:
+    rid: int
+    case: Case
+    steps: int
+    precision: str = "fp64"   # "fp64" or "fp32"
+    arrival: float = 0.0      # seconds after the start of the run
+    t_admit: float | None = None
+    t_done: float | None = None
+    result: dict | None = None
+
+
+def device_bytes_estimate(case: Case, precision: str) -> int:
+    """Device memory a simulation needs on the fused path."""
+    n = case.nx * case.ny * case.nz
+    if precision == "fp64":
+        fields = 24 + (8 if case.lShr else 0)  # U[2], Z, and the right-hand-side block for FT
+        return n * 8 * fields + 64 * 1024
+    return n * (4 * 16 + 8 * 8 + (8 if case.lShr else 0)) + 64 * 1024
+
+
+def poisson_requests(n: int, rate: float, seed: int = 0, grid_min=(32, 32, 32), grid_max=(256, 256, 128),
+                     steps=(50, 2000), fp32_fraction: float = 0.5, re_range=(3e-3, 3e-2),
+                     base: Case | None = None) -> list:
+    """Request stream: Poisson arrivals at `rate` per second, grids
+    log-uniform between grid_min and grid_max (nx = ny), step counts uniform,
+    mixed precision, random seeds and 1/Re log-uniform."""
+    rng = np.random.default_rng(seed)
+    base = base or Case(nPx=32, nPy=32, nPz=32, lMag=True)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        lx = np.exp(rng.uniform(np.log(grid_min[0]), np.log(grid_max[0])))
+        lz = np.exp(rng.uniform(np.log(grid_min[2]), np.log(grid_max[2])))
+        nxy = int(max(grid_min[0], min(grid_max[0], round(lx / 8) * 8)))
+        nz = int(max(grid_min[2], min(grid_max[2], round(lz / 4) * 4)))
+        ore = np.exp(rng.uniform(np.log(re_range[0]), np.log(re_range[1])))
+        case = base.replace(nPx=nxy, nPy=nxy, nPz=nz, seed=int(rng.integers(1 << 30)), RE=float(1.0 / ore),
+                            name=f"req{i}")
+        nsteps = int(rng.integers(steps[0], steps[1] + 1))
+        prec = "fp32" if rng.random() < fp32_fraction else "fp64"
+        out.append(Request(rid=i, case=case, steps=nsteps, precision=prec, arrival=t))
+    return out
+
+
+def init_state(sim, case: Case, precision: str, device_init: bool) -> None:
+    """Initial state of a request: generated on the GPU for FP64 contexts
+    (the host mirror of the same generator for FP32 ones), or numpy's."""
+    if device_init and precision == "fp64":
+        sim.init_on_device()
+    else:
+        sim.upload_state(device_initial_state(case) if device_init else initial_state(case))
+    sim.communicate()
+
+
+class _Resident:
+    def __init__(self, req: Request, sim: Simulation, nbytes: int):
+        self.req = req
+        self.sim = sim
+        self.remaining = req.steps
+        self.nbytes = nbytes
+
+
+class Server:
+    """Admits requests under an HBM budget and steps the resident ones together.
+
+    quantum: at most this many steps are queued per resident simulation
+    between scheduling decisions (admissions and completions happen between
+    quanta).  tile: batch tile shape (None = autotune once, then keep it, so
+    every batch of the run uses the same kernel instance)."""
+
+    def __init__(self, hbm_budget_bytes: int, quantum: int = 25, tile: int | None = None,
+                 keep_results: bool = False, device_init: bool = True):
+        self.budget = int(hbm_budget_bytes)
+        self.quantum = int(quantum)
+        self.tile = tile
+        self.keep_results = keep_results
+        self.device_init = device_init
+        self.used = 0
+        self.resident: dict[int, _Resident] = {}
+        self.batches: dict = {}
+        self.batch_members: dict = {}
+        self.cell_steps = 0
+        self.admissions = 0
+        self.max_resident = 0
+        self.batch_rebuilds = 0
+
+    # -- membership ------------------------------------------------------
+    def _admit(self, req: Request, now: float) -> bool:
+        need = device_bytes_estimate(req.case, req.precision)
+        if self.used + need > self.budget:
+            return False
+        sim = Simulation(req.case, precision=req.precision)
+        init_state(sim, req.case, req.precision, self.device_init)
+        self.used += need
+        req.t_admit = now
+        self.resident[req.rid] = _Resident(req, sim, need)
+        self.admissions += 1
+        self.max_resident = max(self.max_resident, len(self.resident))
+        return True
+
+    def _finish(self, r: _Resident, now: float) -> None:
+        if self.keep_results:
+            r.req.result = r.sim.download_state()
+        else:
+            r.sim.sync()
+        r.sim.close()
+        self.used -= r.nbytes
+        r.req.t_done = now
+        del self.resident[r.req.rid]
+
+    def _groups(self):
+        g = {}
+        for rid, r in self.resident.items():
+            if r.req.precision == "fp64":
+                key = (r.req.case.lMag, r.req.case.lRot, r.req.case.lShr)
+                g.setdefault(key, []).append(rid)
+        return g
+
+    def _sync_batches(self) -> None:
+        groups = self._groups()
+        for key in list(self.batches):
+            if key not in groups or self.batch_members[key] != groups[key]:
+                self.batches[key].close()
+                del self.batches[key]
+                del self.batch_members[key]
+        for key, rids in groups.items():
+            if key not in self.batches:
+                b = Batch([self.resident[r].sim for r in rids])
+                if self.tile is None:
+                    self.tile, _ = b.autotune(report=False)
+                b.set_tile(self.tile)
+                self.batches[key] = b
+                self.batch_members[key] = list(rids)
+                self.batch_rebuilds += 1
+
+    # -- one scheduling quantum --------------------------------------------
+    def _advance(self) -> int:
+        """Queue up to `quantum` steps for every resident simulation; returns
+        how many steps were queued per simulation."""
+        if not self.resident:
+            return 0
+        q = min(self.quantum, min(r.remaining for r in self.resident.values()))
+        for key, b in self.batches.items():
+            b.steps(q)
+        for r in self.resident.values():
+            if r.req.precision != "fp64":
+                r.sim.steps(q, r.req.case.dt)
+        for r in self.resident.values():
+            r.remaining -= q
+            self.cell_steps += r.req.case.cells * q
+        for b in self.batches.values():
+            b.sync()
+        for r in self.resident.values():
+            if r.req.precision != "fp64":
+                r.sim.sync()
+        return q
+
+    def run(self, requests: list, realtime: bool = True, virtual_step_s: float = 1e-3) -> dict:
+        """Serve `requests`.  realtime=False replaces the wall clock by a
+        virtual one that advances virtual_step_s per queued step, so a run's
+        admissions are reproducible."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        future = deque(reqs)
+        waiting: deque = deque()
+        t0 = time.perf_counter()
+        clock = (lambda: time.perf_counter() - t0) if realtime else None
+        virtual = 0.0
+        while future or waiting or self.resident:
+            now = clock() if realtime else virtual
+            while future and future[0].arrival <= now:
+                waiting.append(future.popleft())
+            changed = False
+            while waiting and self._admit(waiting[0], now):
+                waiting.popleft()
+                changed = True
+            if not self.resident:
+                if waiting and not future:
+                    raise RuntimeError(f"request {waiting[0].rid} does not fit the HBM budget on its own")
+                if future:
+                    nxt = future[0].arrival
+                    if realtime:
+                        time.sleep(max(0.0, nxt - clock()))
+                    else:
+                        virtual = nxt
+                continue
+            if changed:
+                self._sync_batches()
+            q = self._advance()
+            if not realtime:
+                virtual += q * virtual_step_s
+            now = clock() if realtime else virtual
+            done = [r for r in self.resident.values() if r.remaining <= 0]
+            for r in done:
+                self._finish(r, now)
+            if done:
+                self._sync_batches()
+        wall = (clock() if realtime else virtual)
+        for b in self.batches.values():
+            b.close()
+        self.batches.clear()
+        tts = np.array([r.t_done - r.arrival for r in reqs])
+        return {"requests": len(reqs), "wall_s": wall, "cell_steps": self.cell_steps,
+                "value": self.cell_steps / wall if wall > 0 else None,
+                "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
+                "max_resident": self.max_resident, "batch_rebuilds": self.batch_rebuilds, "tile": self.tile}
+
+
+def run_serial(requests: list, device_init: bool = True) -> dict:
+    """The same requests one after another on the plain single-instance FP64
+    path (the baseline of the serving form)."""
+    t0 = time.perf_counter()
+    cs = 0
+    for req in requests:
+        sim = Simulation(req.case, precision="fp64")
+        init_state(sim, req.case, "fp64", device_init)
+        sim.steps(req.steps, req.case.dt)
+        sim.sync()
+        sim.close()
+        cs += req.case.cells * req.steps
+    wall = time.perf_counter() - t0
+    return {"wall_s": wall, "cell_steps": cs, "value": cs / wall}

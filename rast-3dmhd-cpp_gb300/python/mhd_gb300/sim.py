@@ -105,6 +105,14 @@ class Simulation:
     def download_state(self) -> dict:
         return {k: self.download(k) for k in STATE_FIELDS[:self.case.nfields]}
 
+    def init_on_device(self) -> None:
+        """The case's synthetic initial state generated on the GPU
+        (case.device_initial_state is its host mirror)."""
+        from .case import z_coordinate
+        zc = np.ascontiguousarray(z_coordinate(self.case), dtype=np.float64)
+        self._ck(self.L.mhd_init_polytrope(self.ctx, _dp(zc), float(self.case.noise), int(self.case.seed) & (2**64 - 1),
+                                           float(self.case.bz0)))
+
     def set_time(self, timt: float, nit: int = 0) -> None:
         self.timt = timt
         self._ck(self.L.mhd_set_time(self.ctx, timt, nit))
@@ -169,3 +177,57 @@ class Simulation:
         if check:
             self._ck(st)
         return d.as_dict()
+
+
+class Batch:
+    """Ragged batch of FP64 fused-path Simulations stepped together
+    (one persistent launch per substage, CUDA-graph step, autotuned tile)."""
+
+    TILES = ("32x4", "32x8", "16x8")
+
+    def __init__(self, sims: list, dts: list | None = None):
+        self.L = abi.load()
+        self.sims = list(sims)
+        n = len(self.sims)
+        ctxs = (C.c_void_p * n)(*[s.ctx.value for s in self.sims])
+        d = np.ascontiguousarray([s.case.dt if dts is None else dts[i] for i, s in enumerate(self.sims)],
+                                 dtype=np.float64)
+        self._dts = d
+        b = C.c_void_p()
+        st = self.L.mhd_batch_create(ctxs, _dp(d), n, None, C.byref(b))
+        if st != abi.MHD_OK:
+            raise abi.MhdError(st, "mhd_batch_create failed")
+        self.b = b
+
+    def close(self) -> None:
+        if getattr(self, "b", None):
+            self.L.mhd_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tile(self, tile: int) -> None:
+        abi.check(self.L.mhd_batch_set_tile(self.b, tile))
+
+    def tile(self) -> int:
+        t = C.c_int()
+        abi.check(self.L.mhd_batch_tile(self.b, C.byref(t)))
+        return t.value
+
+    def autotune(self, report: bool = True) -> tuple[int, list]:
+        chosen = C.c_int()
+        ms = np.zeros(3)
+        abi.check(self.L.mhd_batch_autotune(self.b, C.byref(chosen), _dp(ms) if report else None))
+        return chosen.value, list(ms)
+
+    def steps(self, n: int) -> None:
+        abi.check(self.L.mhd_batch_steps(self.b, n))
+        for s in self.sims:
+            s.timt += n * s.case.dt
+
+    def sync(self) -> None:
+        abi.check(self.L.mhd_batch_sync(self.b))

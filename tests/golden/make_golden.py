@@ -70,6 +70,14 @@ def main() -> None:
         print("wrote", name)
     (HERE / "cases.json").write_text(json.dumps(manifest, indent=1, sort_keys=True))
 
+    # the reference's own dump files (dumpData) of two cases after 3 steps
+    for name in ("mhd_fixedT", "hydro_default_bc"):
+        case = small_cases()[name]
+        d = HERE / f"dat0_{name}"
+        d.mkdir(exist_ok=True)
+        refcase.run(case, initial_state(case), "dump", 3, dump_prefix=str((d / "test").resolve()))
+        print("wrote", d)
+
     c0 = config0()
     st = initial_state(c0)
     r = refcase.run(c0, st, "steps", 100)

@@ -111,3 +111,21 @@ def test_nan_state_is_reported():
     with pytest.raises(MhdError):
         sim.diagnostics()
     sim.close()
+
+
+def test_device_initial_state_matches_host_mirror():
+    from mhd_gb300.case import device_initial_state
+    case = small_cases()["mhd_rot_shr"].replace(nPx=24, nPy=10, nPz=8, seed=12345)
+    sim = Simulation(case, path="fused")
+    sim.init_on_device()
+    got = sim.download_state()
+    sim.close()
+    want = device_initial_state(case)
+    for k in STATE_FIELDS:
+        scale = max(np.abs(want[k]).max(), 1e-300)
+        assert np.abs(got[k] - want[k]).max() / scale <= 1e-13, k
+    # the noise is a standard normal sample
+    from mhd_gb300.case import z_coordinate
+    t1 = 1.0 + case.THETA * z_coordinate(case)
+    g = (want["TT"][1:-1, 1:-1, 1:-1] / t1[1:-1, None, None] - 1) / case.noise
+    assert abs(g.mean()) < 0.2 and 0.8 < g.std() < 1.2

@@ -1,0 +1,163 @@
+"""Host-side logic without a GPU: the request stream, the continuous-batching
+scheduler on a fake device backend, and the multi-rank (replica) reductions
+of bench.py over two gloo ranks."""
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+from mhd_gb300 import serve
+from mhd_gb300.serve import Request, Server, device_bytes_estimate, poisson_requests
+
+
+def test_poisson_requests_are_reproducible_and_in_range():
+    a = poisson_requests(50, rate=20.0, seed=3)
+    b = poisson_requests(50, rate=20.0, seed=3)
+    assert [(r.case.nPx, r.case.nPz, r.steps, r.precision, r.arrival) for r in a] == \
+           [(r.case.nPx, r.case.nPz, r.steps, r.precision, r.arrival) for r in b]
+    arr = np.array([r.arrival for r in a])
+    assert np.all(np.diff(arr) > 0)
+    assert all(32 <= r.case.nPx <= 256 and r.case.nPx == r.case.nPy and 32 <= r.case.nPz <= 128 for r in a)
+    assert all(50 <= r.steps <= 2000 for r in a)
+    assert all(1 / 3e-2 - 1e-9 <= r.case.RE <= 1 / 3e-3 + 1e-9 for r in a)
+    assert {r.precision for r in a} == {"fp32", "fp64"}
+
+
+class FakeSim:
+    live = 0
+
+    def __init__(self, case, precision="fp64", **kw):
+        self.case, self.precision, self.steps_done, self.timt = case, precision, 0, 0.0
+        FakeSim.live += 1
+
+    def upload_state(self, st):
+        pass
+
+    def init_on_device(self):
+        pass
+
+    def communicate(self):
+        pass
+
+    def steps(self, n, dt=None):
+        self.steps_done += n
+
+    def sync(self):
+        pass
+
+    def download_state(self):
+        return {"steps": self.steps_done}
+
+    def close(self):
+        FakeSim.live -= 1
+
+
+class FakeBatch:
+    def __init__(self, sims):
+        self.sims = sims
+
+    def autotune(self, report=True):
+        return 1, [1.0, 0.5, 0.7]
+
+    def set_tile(self, t):
+        self.t = t
+
+    def steps(self, n):
+        for s in self.sims:
+            s.steps_done += n
+
+    def sync(self):
+        pass
+
+    def close(self):
+        pass
+
+
+@pytest.fixture
+def fake_backend(monkeypatch):
+    monkeypatch.setattr(serve, "Simulation", FakeSim)
+    monkeypatch.setattr(serve, "Batch", FakeBatch)
+    monkeypatch.setattr(serve, "initial_state", lambda case: {})
+    monkeypatch.setattr(serve, "device_initial_state", lambda case: {})
+    FakeSim.live = 0
+    yield
+
+
+def test_scheduler_admits_under_budget_and_completes_every_request(fake_backend):
+    reqs = poisson_requests(40, rate=100.0, seed=1, grid_min=(16, 16, 8), grid_max=(64, 64, 32), steps=(3, 40))
+    sizes = [device_bytes_estimate(r.case, r.precision) for r in reqs]
+    budget = sum(sorted(sizes)[-3:])
+    srv = Server(budget, quantum=5, keep_results=True)
+    used_peak = [0]
+    orig = srv._admit
+
+    def spy(req, now):
+        ok = orig(req, now)
+        used_peak[0] = max(used_peak[0], srv.used)
+        return ok
+    srv._admit = spy
+    st = srv.run(reqs, realtime=False)
+    assert used_peak[0] <= budget
+    assert FakeSim.live == 0 and srv.used == 0
+    assert all(r.result["steps"] == r.steps for r in reqs)          # each ran exactly its step count
+    assert all(r.t_done >= r.t_admit >= r.arrival for r in reqs)
+    assert st["max_resident"] >= 2 and st["tile"] == 1
+    assert st["tts_p99_s"] >= st["tts_p50_s"] > 0
+
+
+def test_scheduler_rejects_a_request_larger_than_the_budget(fake_backend):
+    big = Request(rid=0, case=poisson_requests(1, 1.0, seed=2)[0].case, steps=3)
+    with pytest.raises(RuntimeError):
+        Server(10, quantum=5).run([big], realtime=False)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _rank_main(rank, world, port, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(REPO))
+    import bench
+    d = bench.Dist()
+    d.barrier()
+    m = d.max(float(rank + 1) * 1.5)
+    d.close()
+    q.put((rank, m))
+
+
+def test_bench_replica_reductions_two_gloo_ranks():
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out = [q.get(timeout=120) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert sorted(out) == [(0, 3.0), (1, 3.0)]
+
+
+def test_device_initial_state_mirror_is_a_seeded_gaussian():
+    from mhd_gb300.case import device_initial_state, small_cases, z_coordinate
+    c = small_cases()["mhd_fixedT"].replace(nPx=32, nPy=32, nPz=16, seed=5)
+    a, b = device_initial_state(c), device_initial_state(c)
+    assert all(np.array_equal(a[k], b[k]) for k in a)
+    t1 = 1 + c.THETA * z_coordinate(c)
+    g = (a["TT"][1:-1, 1:-1, 1:-1] / t1[1:-1, None, None] - 1) / c.noise
+    assert abs(g.mean()) < 0.02 and abs(g.std() - 1) < 0.02
+    d = device_initial_state(c.replace(seed=6))
+    assert not np.array_equal(a["TT"], d["TT"])
+    # periodic ghosts
+    assert np.array_equal(a["TT"][:, 0, :], a["TT"][:, -2, :]) and np.array_equal(a["TT"][:, :, -1], a["TT"][:, :, 1])

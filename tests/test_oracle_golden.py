@@ -78,3 +78,35 @@ def test_unsupported_wall_condition_is_rejected():
     sim = oracle_from_fixture(case.replace(TP=0.1), g)
     with pytest.raises(ValueError):
         sim.BCON()
+
+
+@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc"])
+def test_dat0_writer_matches_reference_dump(name, tmp_path):
+    """mhd_write_dat0 (host code of the library) writes the same bytes as the
+    reference's dumpData for the same state (3 steps of the golden case, 2x2 ranks)."""
+    import ctypes as C
+    from mhd_gb300 import abi
+    import sys
+    sys.path.insert(0, str(GOLDEN.parent.parent / "rast-3dmhd-cpp_gb300"))
+    import build as mhd_build
+    mhd_build.build()
+    L = abi.load()
+    case, g = load_golden(name)
+    nf = case.nfields
+    state = np.ascontiguousarray(np.stack([g["steps3_" + k] for k in STATE_FIELDS[:nf]]))
+    prefix = str(tmp_path / "mine")
+    rc = L.mhd_write_dat0(prefix.encode(), case.nPx, case.nPy, case.nPz, nf,
+                          state.ctypes.data_as(C.POINTER(C.c_double)), case.nPEy, case.nPEz, 0)
+    assert rc == 0
+    for rank in range(case.nPEy * case.nPEz):
+        ref = (GOLDEN / f"dat0_{name}" / f"test.dat0.{rank:04d}").read_bytes()
+        mine = (tmp_path / f"mine.dat0.{rank:04d}").read_bytes()
+        assert mine == ref, rank
+    # read it back (a later record keeps the first one)
+    rc = L.mhd_write_dat0(prefix.encode(), case.nPx, case.nPy, case.nPz, nf,
+                          state.ctypes.data_as(C.POINTER(C.c_double)), case.nPEy, case.nPEz, 1)
+    back = np.zeros_like(state)
+    assert L.mhd_read_dat0(prefix.encode(), case.nPx, case.nPy, case.nPz, nf,
+                           back.ctypes.data_as(C.POINTER(C.c_double)), case.nPEy, case.nPEz, 0) == 0
+    I = np.s_[:, 1:-1, 1:-1, 1:-1]
+    assert np.array_equal(back[I], state[I])
