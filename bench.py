@@ -258,6 +258,16 @@ def run_ours(args, dist: Dist) -> None:
     ms_max = dist.max(ms)
     value = dist.world * case.cells * args.steps / (ms_max / 1e3)
 
+    # the reference's run mode: a CFL dt for every step, reduced on the device
+    # into the record the substage kernels read (mhd_steps_cfl)
+    sim.steps_cfl(1)
+    sim.timer_start()
+    _, dcfl = sim.steps_cfl(args.steps)
+    ms_cfl = dist.max(sim.timer_stop())
+    cfl_mode = {"value": dist.world * case.cells * args.steps / (ms_cfl / 1e3), "ms_per_step": ms_cfl / args.steps,
+                "cost_vs_fixed_dt": ms_cfl / ms_max - 1.0, "last_dt": dcfl["dt"],
+                "path": "mhd_steps_cfl: CFL reduction + 3 fused substages + BCON per step, one host sync per call"}
+
     # roofline of the fused substage kernel
     bytes_cell_step = algorithmic_bytes_per_cell_step(case)
     per_launch_bytes = case.cells * bytes_cell_step / 3.0
@@ -330,6 +340,7 @@ def run_ours(args, dist: Dist) -> None:
                  "inst_per_cell_substage": inst_cell, "peak_tflops_measured": fp64_peak.value,
                  "note": "the FP64 pipe (measured DFMA roof), not HBM, bounds the fused FP64 kernel on GB300"},
         "clocks": clk,
+        "adaptive_cfl": cfl_mode,
     }
     if cpu:
         line["cpu_baseline"] = cpu
@@ -444,7 +455,28 @@ def run_batch(args, dist: Dist) -> None:
     serial_secs = (time.perf_counter() - t) * nsteps / serial_steps
     for s in sims:
         s.close()
+    # the same instances with FP32 storage, batched
+    sims32 = []
+    for c in cases:
+        s = Simulation(c, precision="fp32")
+        s.upload_state(initial_state(c))
+        s.communicate()
+        sims32.append(s)
+    b32 = Batch(sims32)
+    b32.set_tile(0)
+    b32.steps(3)
+    b32.sync()
+    t = time.perf_counter()
+    b32.steps(nsteps)
+    b32.sync()
+    secs32 = time.perf_counter() - t
+    b32.close()
+    for s in sims32:
+        s.close()
     out = {"form": "batch", "metric": METRIC, "unit": METRIC, "instances": len(cases), "steps": nsteps,
+           "fp32_storage_batched": {"value": cells * nsteps / secs32, "ms_per_step": 1e3 * secs32 / nsteps,
+                                    "vs_plain_fp64_serial": serial_secs / secs32,
+                                    "vs_fp64_batched": secs / secs32},
            "cells_per_step": cells, "dtype": "f64",
            "value": cells * nsteps / secs, "ms_per_step": 1e3 * secs / nsteps,
            "autotune": {"chosen": ["32x4", "32x8", "16x8"][chosen], "ms_per_step_by_tile": tile_ms},

@@ -208,13 +208,24 @@ int mhd_fluxes_noalloc(const mhd_fluxes_noalloc_args* args, void* stream);
 int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out);
 /* n fixed-dt steps queued without host synchronisation. */
 int mhd_steps(mhd_ctx* ctx, int n, double dt);
+/* n steps of the reference's run mode, each with its CFL dt (step(),
+ * 3dmhdsub.h:36-106, called from the loop of 3dmhd.cpp:271-331).  On the
+ * fused FP64 path the dt is reduced into a device-resident record that the
+ * substage kernels read, so the n steps are queued without host round trips
+ * and the call blocks once, at the end (the FP32-storage and parity paths
+ * read dt back each step).  dt agrees bit for bit with mhd_cfl_dt.  When a
+ * step's dt falls below 1e-8 (the halt of 3dmhd.cpp:292) the state stays as
+ * it was before that step and the call returns MHD_ERR_DT_TOO_SMALL
+ * (MHD_ERR_NUMERIC for a non-finite dt).  `out` (may be NULL) receives the
+ * dt of the last step computed, umach, timt and nit. */
+int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out);
 /* Mass, energy, max|div B| and sanity flags of the current state (blocks). */
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
 int mhd_sync(mhd_ctx* ctx);
 
 /* ---- ragged batches ------------------------------------------------------ */
-/* n independent FP64 instances (fused-path contexts with one switch set, any
- * sizes) stepped together: each RK3 substage is one persistent launch over
+/* n independent instances (fused-path contexts with one switch set and one
+ * precision, any sizes) stepped together: each RK3 substage is one persistent launch over
  * the tiles of all instances, the whole step is a CUDA graph, and the tile
  * shape is picked by timing every candidate on a scratch copy of the batch
  * (cached per batch signature).  No counterpart in the reference, which runs
@@ -224,7 +235,8 @@ int mhd_sync(mhd_ctx* ctx);
 typedef struct mhd_batch mhd_batch;
 int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* stream, mhd_batch** out);
 int mhd_batch_destroy(mhd_batch* b);
-/* tile shape: -1 = autotune on the next step, 0 = 32x4, 1 = 32x8, 2 = 16x8 */
+/* tile shape: -1 = autotune on the next step, 0 = 32x4, 1 = 32x8, 2 = 16x8
+ * (FP32-storage batches always use 32x8) */
 int mhd_batch_set_tile(mhd_batch* b, int tile);
 int mhd_batch_tile(const mhd_batch* b, int* tile);
 /* Time every tile shape (ms_per_step, may be NULL, gets one entry per shape)

@@ -154,7 +154,9 @@ int ensure_parity_buffers(mhd_ctx* ctx) {
     return alloc_block(ctx, &ctx->Sb, 4);
 }
 
-int fused_step(mhd_ctx* ctx, double dt) {
+// One fused FP64 step; dtp (device) = the time-step record of mhd_steps_cfl,
+// from which the kernels read dt, or null for the host dt.
+int fused_step(mhd_ctx* ctx, double dt, const double* dtp = nullptr) {
     int rc = ensure_u1(ctx);
     if (rc) return rc;
     if (ctx->sw & kSwShr) {
@@ -176,6 +178,9 @@ int fused_step(mhd_ctx* ctx, double dt) {
         a.FT = ctx->Fb ? ctx->Fb + (size_t)F_FT * ctx->ncell : nullptr;
         a.gdt = gam[s] * dt;
         a.zdt = zet[s] * dt;
+        a.dtp = dtp;
+        a.gam = gam[s];
+        a.zet = zet[s];
         a.substage = s;
         cudaEvent_t* ev = nullptr;
         if (ctx->profiling) {
@@ -355,6 +360,19 @@ int fused32_step(mhd_ctx* ctx, double dt) {
 }  // namespace
 
 namespace mhd::ctxops {
+void advance_time(mhd_ctx* c, double dt) {
+    c->nit += 1;
+    c->timc += dt;
+    c->timt = c->timi + c->timc;
+    c->last_dt = dt;
+}
+int ensure_u32_1(mhd_ctx* ctx) {
+    int rc = ::alloc_f32(ctx, &ctx->U32[1]);
+    if (!rc && (ctx->sw & kSwShr) && !ctx->FT64) rc = ::alloc_block(ctx, &ctx->FT64, 1);
+    return rc;
+}
+int sync_zghosts32(mhd_ctx* ctx) { return ::sync_zghosts32(ctx); }
+Fields8f fields32_of(const mhd_ctx* c, float* base) { return ::fields32_of(c, base); }
 int ensure_u1(mhd_ctx* ctx) { return ::ensure_u1(ctx); }
 int sync_zghosts(mhd_ctx* ctx) { return ::sync_zghosts(ctx); }
 int alloc_block(mhd_ctx* ctx, double** p, int nfields) { return ::alloc_block(ctx, p, nfields); }
@@ -497,16 +515,17 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     if (!arc) arc = alloc_block(ctx, &ctx->Zb, 8);
     if (!arc && ctx->fp32 && (ctx->sw & kSwShr)) arc = alloc_block(ctx, &ctx->FT64, 1);
     if (!arc && cudaMalloc(&ctx->red, sizeof(double) * 8 * (size_t)ctx->red_blocks) != cudaSuccess) arc = MHD_ERR_NOMEM;
-    if (!arc && cudaMalloc(&ctx->d_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
-    if (!arc && cudaMallocHost(&ctx->h_out, sizeof(double) * 8) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    // d_out: 8 doubles of reduction results, then the kDtRecord-double time-step record
+    if (!arc && cudaMalloc(&ctx->d_out, sizeof(double) * (8 + kDtRecord)) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    if (!arc && cudaMallocHost(&ctx->h_out, sizeof(double) * (8 + kDtRecord)) != cudaSuccess) arc = MHD_ERR_NOMEM;
     if (arc) {
         cudaGetLastError();
         fprintf(stderr, "mhd_create: %s\n", ctx->err.empty() ? "allocation failed" : ctx->err.c_str());
         mhd_destroy(ctx);
         return MHD_ERR_NOMEM;
     }
-    ctx->bytes += sizeof(double) * (8 * (size_t)ctx->red_blocks + 8);
-    ctx->timt = 0.0;
+    ctx->bytes += sizeof(double) * (8 * (size_t)ctx->red_blocks + 8 + kDtRecord);
+    ctx->timt = ctx->timi = ctx->timc = 0.0;
     ctx->nit = 0;
     *out = ctx;
     return MHD_OK;
@@ -629,7 +648,10 @@ int mhd_download_state(mhd_ctx* ctx, double* host) {
 
 int mhd_set_time(mhd_ctx* ctx, double timt, long long nit) {
     if (!ctx) return MHD_ERR_INVALID;
+    // a restart: TIMI = the restored time, TIMC counts from 0 (3dmhd.cpp:114,460)
     ctx->timt = timt;
+    ctx->timi = timt;
+    ctx->timc = 0.0;
     ctx->nit = nit;
     return MHD_OK;
 }
@@ -731,10 +753,7 @@ int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out) {
     }
     rc = ctx->fp32 ? fused32_step(ctx, dt) : ctx->prm.path == MHD_PATH_PARITY ? parity_step(ctx, dt) : fused_step(ctx, dt);
     if (rc) return rc;
-    // 3dmhdsub.h:150-152 (TIMI + TIMC accumulates the same way)
-    ctx->nit += 1;
-    ctx->timt += dt;
-    ctx->last_dt = dt;
+    ctxops::advance_time(ctx, dt);
     if (out) {
         memset(out, 0, sizeof(*out));
         out->dt = dt;
@@ -750,6 +769,61 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt) {
     for (int s = 0; s < n; s++) {
         int rc = mhd_step(ctx, dt, nullptr);
         if (rc) return rc;
+    }
+    return MHD_OK;
+}
+
+int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out) {
+    if (!ctx || n < 0) return MHD_ERR_INVALID;
+    if (out) memset(out, 0, sizeof(*out));
+    if (ctx->fp32 || ctx->prm.path == MHD_PATH_PARITY) {
+        // these paths read the CFL dt back every step
+        mhd_diag d{};
+        for (int s = 0; s < n; s++) {
+            const int rc = mhd_step(ctx, 0.0, &d);
+            if (out) *out = d;
+            if (rc) return rc;
+        }
+        return MHD_OK;
+    }
+    double* rec = ctx->d_out + 8;
+    double* h = ctx->h_out + 8;
+    for (int k = 0; k < kDtRecord; k++) h[k] = 0.0;
+    h[1] = ctx->timt;
+    h[6] = ctx->timi;
+    h[7] = ctx->timc;
+    CK(cudaMemcpyAsync(rec, h, sizeof(double) * kDtRecord, cudaMemcpyHostToDevice, ctx->stream));
+    const bool mag = (ctx->sw & kSwMag) != 0;
+    for (int s = 0; s < n; s++) {
+        int rc = ensure_u1(ctx);
+        if (!rc) rc = sync_zghosts(ctx);
+        if (rc) return rc;
+        const int e = cfl_dt_on_device(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red,
+                                       ctx->red_blocks, rec, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "CFL launch");
+        // BCON reads TIMT only through cos(0 * TIMT) = 1 (3dmhdsub.h:725,732,824), so the
+        // host's TIMT at the call stands in for the device's
+        rc = fused_step(ctx, 0.0, rec);
+        if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(h, rec, sizeof(double) * kDtRecord, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const long long done = (long long)h[5];
+    ctx->timt = h[1];
+    ctx->timc = h[7];
+    ctx->nit += done;
+    ctx->last_umach = h[2];
+    if (done > 0 || h[3] != 0.0) ctx->last_dt = h[4];
+    if (out) {
+        out->dt = ctx->last_dt;
+        out->umach = ctx->last_umach;
+        out->timt = ctx->timt;
+        out->nit = ctx->nit;
+    }
+    if (h[3] != 0.0) {
+        if (!(h[4] == h[4]) || !(h[2] == h[2])) return fail(ctx, MHD_ERR_NUMERIC, "non-finite CFL estimate");
+        return fail(ctx, MHD_ERR_DT_TOO_SMALL,
+                    "DT too small, halt after step " + std::to_string(ctx->nit) + " (3dmhd.cpp:292-331)");
     }
     return MHD_OK;
 }

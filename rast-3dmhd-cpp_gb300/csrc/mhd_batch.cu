@@ -29,7 +29,9 @@ struct mhd_batch {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int tile = -1;  // chosen tile shape
-    bool uxy = true;  // every instance has uniform x/y grids
+    bool uxy = true;   // every instance has uniform x/y grids
+    bool fp32 = false; // FP32-storage instances (one tile shape, 32x8)
+    Fused32Args* d_args32 = nullptr;  // [2][3][n] for FP32 batches
     FusedArgs* d_args = nullptr;  // [2 parities][3 substages][n]
     int4* d_items = nullptr;
     int nitems = 0;
@@ -103,10 +105,45 @@ void fill_args(const mhd_batch* b, const std::vector<double*>& U0, const std::ve
             }
 }
 
+void fill_args32(const mhd_batch* b, const std::vector<int>& cur0, std::vector<Fused32Args>& out) {
+    const int n = (int)b->ctx.size();
+    out.assign((size_t)6 * n, Fused32Args{});
+    for (int p = 0; p < 2; p++)
+        for (int s = 0; s < 3; s++)
+            for (int i = 0; i < n; i++) {
+                const mhd_ctx* c = b->ctx[i];
+                const double gam[3] = {c->k.GAM1, c->k.GAM2, c->k.GAM3};
+                const double zet[3] = {c->k.ZETA1, c->k.ZETA2, 0.0};
+                const int cur = cur0[i] ^ ((3 * p + s) & 1);
+                const int nz = c->g.nz;
+                Fused32Args& a = out[((size_t)p * 3 + s) * n + i];
+                a.g = c->g;
+                a.c = c->c;
+                a.k = c->coef;
+                a.U = ctxops::fields32_of(c, c->U32[cur]);
+                a.Uo = ctxops::fields32_of(c, c->U32[1 - cur]);
+                a.Z = ctxops::fields_of(c, c->Zb);
+                a.FT = c->FT64;
+                a.bgR = c->d_bg;
+                a.bgT = c->d_bg + nz;
+                a.dzT0 = c->d_bg + 2 * nz;
+                a.d2zT0 = c->d_bg + 3 * nz;
+                a.gdt = gam[s] * b->dt[i];
+                a.zdt = zet[s] * b->dt[i];
+                a.timt = c->timt;
+                a.substage = s;
+            }
+}
+
 // Work items for a tile shape: (instance, tile x, tile y), largest z first.
 void make_items(const mhd_batch* b, int tile, std::vector<int4>& items) {
     int tx, ty;
-    batch_tile_dims(tile, &tx, &ty);
+    if (b->fp32) {
+        tx = kBatch32TX;
+        ty = kBatch32TY;
+    } else {
+        batch_tile_dims(tile, &tx, &ty);
+    }
     std::vector<int> order(b->ctx.size());
     for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
@@ -139,7 +176,9 @@ int persistent_grid(mhd_batch* b, int tile, int nitems) {
     int dev = 0, sms = 0, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int rc = b->uxy ? fused_batch_occupancy_uxy(b->sw, tile, &per_sm) : fused_batch_occupancy_gen(b->sw, tile, &per_sm);
+    const int rc = b->fp32 ? fused32_batch_occupancy(b->sw, &per_sm)
+                   : b->uxy ? fused_batch_occupancy_uxy(b->sw, tile, &per_sm)
+                            : fused_batch_occupancy_gen(b->sw, tile, &per_sm);
     if (rc != 0 || per_sm < 1) per_sm = 1;
     return std::max(1, std::min(nitems, sms * per_sm));
 }
@@ -155,6 +194,12 @@ int capture(mhd_batch* b, int tile, FusedArgs* d_args, int4* d_items, int nitems
         cudaMemsetAsync(d_counters + 3 * p, 0, 3 * sizeof(int), b->stream);
         int rc = 0;
         for (int s = 0; s < 3 && !rc; s++) {
+            if (b->fp32) {
+                const Fused32Args* a32 = b->d_args32 + ((size_t)p * 3 + s) * n;
+                rc = fused32_batch_substage(b->sw, a32, d_items, nitems, d_counters + 3 * p + s, grid, b->stream);
+                if (!rc) rc = fused32_batch_bcon(b->sw, a32, b->d_bitems, b->nbitems, b->stream);
+                continue;
+            }
             const FusedArgs* args = d_args + ((size_t)p * 3 + s) * n;
             rc = b->uxy ? fused_batch_substage_uxy(b->sw, tile, args, d_items, nitems, d_counters + 3 * p + s, grid, b->stream)
                         : fused_batch_substage_gen(b->sw, tile, args, d_items, nitems, d_counters + 3 * p + s, grid, b->stream);
@@ -184,9 +229,15 @@ int build(mhd_batch* b) {
     std::vector<int> cur(n);
     for (int i = 0; i < n; i++) {
         mhd_ctx* c = b->ctx[i];
-        int rc = ctxops::ensure_u1(c);
-        if (!rc && (c->sw & kSwShr)) rc = ctxops::alloc_block(c, &c->Fb, 8);
-        if (!rc) rc = ctxops::sync_zghosts(c);
+        int rc;
+        if (b->fp32) {
+            rc = ctxops::ensure_u32_1(c);
+            if (!rc) rc = ctxops::sync_zghosts32(c);
+        } else {
+            rc = ctxops::ensure_u1(c);
+            if (!rc && (c->sw & kSwShr)) rc = ctxops::alloc_block(c, &c->Fb, 8);
+            if (!rc) rc = ctxops::sync_zghosts(c);
+        }
         if (rc) return bfail(b, rc, "instance " + std::to_string(i) + ": " + c->err);
         BCK(cudaStreamSynchronize(c->stream));
         U0[i] = c->U[0];
@@ -195,9 +246,15 @@ int build(mhd_batch* b) {
         FT[i] = c->Fb ? c->Fb + (size_t)F_FT * c->ncell : nullptr;
         cur[i] = c->cur;
     }
-    std::vector<FusedArgs> args;
-    fill_args(b, U0, U1, Z, FT, cur, args);
-    BCK(cudaMemcpy(b->d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice));
+    if (b->fp32) {
+        std::vector<Fused32Args> a32;
+        fill_args32(b, cur, a32);
+        BCK(cudaMemcpy(b->d_args32, a32.data(), sizeof(Fused32Args) * a32.size(), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<FusedArgs> args;
+        fill_args(b, U0, U1, Z, FT, cur, args);
+        BCK(cudaMemcpy(b->d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice));
+    }
     std::vector<int4> items;
     make_items(b, b->tile, items);
     cudaFree(b->d_items);
@@ -308,17 +365,18 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
             delete b;
             return MHD_ERR_INVALID;
         }
-        if (c->fp32 || c->prm.path != MHD_PATH_FUSED) {
+        if (c->prm.path != MHD_PATH_FUSED) {
             delete b;
-            fprintf(stderr, "mhd_batch_create: instances must be FP64 contexts on the fused path\n");
+            fprintf(stderr, "mhd_batch_create: instances must be fused-path contexts\n");
             return MHD_ERR_UNSUPPORTED;
         }
-        if (i > 0 && c->sw != b->sw) {
+        if (i > 0 && (c->sw != b->sw || c->fp32 != b->fp32)) {
             delete b;
             fprintf(stderr, "mhd_batch_create: all instances of a batch need the same switch set\n");
             return MHD_ERR_UNSUPPORTED;
         }
         b->sw = c->sw;
+        b->fp32 = c->fp32;
         b->uxy = b->uxy && c->coef.uniform_xy;
         b->ctx.push_back(c);
         b->dt.push_back(dts[i]);
@@ -335,6 +393,7 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
     make_bcon_items(b, bitems);
     b->nbitems = (int)bitems.size();
     if (cudaMalloc(&b->d_args, sizeof(FusedArgs) * 6 * n) != cudaSuccess ||
+        cudaMalloc(&b->d_args32, sizeof(Fused32Args) * 6 * n) != cudaSuccess ||
         cudaMalloc(&b->d_counters, sizeof(int) * 6) != cudaSuccess ||
         cudaMalloc(&b->d_bitems, sizeof(int2) * bitems.size()) != cudaSuccess ||
         cudaMemcpy(b->d_bitems, bitems.data(), sizeof(int2) * bitems.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -352,6 +411,7 @@ int mhd_batch_destroy(mhd_batch* b) {
     drop_graphs(b->exec);
     if (b->order) cudaEventDestroy(b->order);
     cudaFree(b->d_args);
+    cudaFree(b->d_args32);
     cudaFree(b->d_items);
     cudaFree(b->d_bitems);
     cudaFree(b->d_counters);
@@ -369,6 +429,14 @@ int mhd_batch_set_tile(mhd_batch* b, int tile) {
 
 int mhd_batch_autotune(mhd_batch* b, int* chosen, double* ms_per_step) {
     if (!b) return MHD_ERR_INVALID;
+    if (b->fp32) {  // one tile shape for FP32 storage: nothing to choose
+        b->tile = 0;
+        b->built = false;
+        if (chosen) *chosen = 0;
+        if (ms_per_step)
+            for (int t = 0; t < kBatchTiles; t++) ms_per_step[t] = 0.0;
+        return MHD_OK;
+    }
     const std::string sig = signature(b);
     int best = -1;
     if (!ms_per_step) {
@@ -395,7 +463,8 @@ int mhd_batch_steps(mhd_batch* b, int nsteps) {
         if (rc) return rc;
     }
     bool stale = !b->built;
-    for (size_t i = 0; i < b->ctx.size() && !stale; i++) stale = b->ctx[i]->cur != b->expect_cur[i] || !b->ctx[i]->ghosts_synced;
+    for (size_t i = 0; i < b->ctx.size() && !stale; i++)
+        stale = b->ctx[i]->cur != b->expect_cur[i] || !b->ctx[i]->ghosts_synced;
     if (stale) {
         int rc = build(b);
         if (rc) return rc;
@@ -413,9 +482,7 @@ int mhd_batch_steps(mhd_batch* b, int nsteps) {
             mhd_ctx* c = b->ctx[i];
             c->cur ^= 1;
             b->expect_cur[i] ^= 1;
-            c->nit += 1;
-            c->timt += b->dt[i];
-            c->last_dt = b->dt[i];
+            ctxops::advance_time(c, b->dt[i]);
         }
         b->steps_done++;
     }

@@ -101,7 +101,17 @@ struct FusedArgs {
     double zdt;    // ZETA_k * dt
     double timt;   // simulation time seen by BCON
     int substage;  // 0, 1, 2
+    // device-resident time step (adaptive CFL without a host round trip):
+    // when dtp is set, gdt = gam * dtp[0] and zdt = zet * dtp[0]
+    const double* dtp;
+    double gam, zet;
 };
+// Device time-step record of mhd_steps_cfl: [0] DT in use (0 once halted),
+// [1] TIMT, [2] UMACH, [3] halt flag (DT < 1e-8), [4] the CFL DT computed
+// last, [5] completed steps, [6] TIMI, [7] TIMC.
+constexpr int kDtRecord = 8;
+int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+                     double* rec, cudaStream_t st);
 int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st);
 // Ragged batches: persistent CTAs take (instance, tile x, tile y) items from a
 // counter that must be zero at launch.  Tile shapes: 0 = 32x4, 1 = 32x8, 2 = 16x8.
@@ -134,12 +144,20 @@ struct Fused32Args {
     const double *bgR, *bgT;     // reference profiles rho0(z), T0(z)
     const double *dzT0, *d2zT0;  // their premultiplied first and second z derivatives
     double gdt, zdt;
+    double timt;
     int substage;
 };
 int fused32_substage(unsigned sw, const Fused32Args& a, cudaStream_t st);
 int fused32_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const double* bgR,
                        const double* bgT, double timt, cudaStream_t st);
 int communicate32(int nf, const Grid& g, Fields8f U, cudaStream_t st);
+// ragged batches of FP32-storage instances (tile 32x8; same item and counter
+// conventions as the FP64 batch)
+constexpr int kBatch32TX = 32, kBatch32TY = 8;
+int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter, int grid,
+                           cudaStream_t st);
+int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm);
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st);
 int cfl32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT, double* partials,
           int max_blocks, double* out5, cudaStream_t st);
 int diag32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,

@@ -31,7 +31,9 @@ struct mhd_ctx {
     double* h_out = nullptr; // pinned mirror of d_out
     int red_blocks = 0;
     bool ghosts_synced = false;  // z ghost planes of U[1-cur] match U[cur]
-    double timt = 0.0;
+    // simulation time as step() keeps it (3dmhdsub.h:150-152): TIMC sums the
+    // steps' DT, TIMT = TIMI + TIMC
+    double timt = 0.0, timi = 0.0, timc = 0.0;
     long long nit = 0;
     double last_dt = 0.0, last_umach = 0.0;
     size_t bytes = 0;
@@ -50,9 +52,14 @@ struct mhd_ctx {
 };
 
 namespace mhd::ctxops {
+int ensure_u32_1(mhd_ctx* ctx);
+int sync_zghosts32(mhd_ctx* ctx);
+Fields8f fields32_of(const mhd_ctx* c, float* base);
 int ensure_u1(mhd_ctx* ctx);
 int sync_zghosts(mhd_ctx* ctx);
 int alloc_block(mhd_ctx* ctx, double** p, int nfields);
 Fields8 fields_of(const mhd_ctx* c, double* base);
 int fail(mhd_ctx* c, int code, const std::string& msg);
+// one completed step of length dt: nIt, TIMC and TIMT advance as 3dmhdsub.h:150-152
+void advance_time(mhd_ctx* c, double dt);
 }  // namespace mhd::ctxops

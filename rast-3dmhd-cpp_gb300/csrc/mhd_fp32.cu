@@ -98,13 +98,14 @@ __device__ __forceinline__ void store32_with_images(float* F, const Grid& g, int
     }
 }
 
+// One tile (bx, by) of one instance, interior z planes [zb, ze).
 template <class SW>
-__global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
+__device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, int by, int zb, int ze,
+                                                unsigned char* ring) {
     constexpr int NQ = nqf<SW>();
-    extern __shared__ __align__(16) unsigned char ring[];
     const Grid& g = a.g;
     const Consts& c = a.c;
-    const int x0 = 1 + blockIdx.x * kTX, y0 = 1 + blockIdx.y * kTY;
+    const int x0 = 1 + bx * kTX, y0 = 1 + by * kTY;
     const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
     const int x = x0 + tx, y = y0 + ty;
     const bool active = (x <= g.nx - 2) && (y <= g.ny - 2);
@@ -122,10 +123,6 @@ __global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
     const float tmpc = (float)(c.OCV / c.REPR);
     const float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
 
-    // z range of this CTA: chunk blockIdx.z of gridDim.z
-    const int nPz = g.nz - 2;
-    const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);
-    const int ze = 1 + (int)((long long)nPz * (blockIdx.z + 1) / gridDim.z);
     load_plane32<SW>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
     load_plane32<SW>(a, ring, zb % 3, zb, x0, y0);
     load_plane32<SW>(a, ring, (zb + 1) % 3, zb + 1, x0, y0);
@@ -318,17 +315,41 @@ __global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
     }
 }
 
+// one instance: grid (x tiles, y tiles, z chunks)
+template <class SW>
+__global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
+    extern __shared__ __align__(16) unsigned char ring[];
+    const int nPz = a.g.nz - 2;
+    const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);
+    const int ze = 1 + (int)((long long)nPz * (blockIdx.z + 1) / gridDim.z);
+    substage32_tile<SW>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
+}
+
+// ragged batch: persistent CTAs take (instance, tile x, tile y, z range) items
+// (w = first plane | end plane << 16) from a counter that is zero at launch
+template <class SW>
+__global__ void __launch_bounds__(kThreads) k_substage32_batch(const Fused32Args* __restrict__ args,
+                                                               const int4* __restrict__ items, int nitems,
+                                                               int* counter) {
+    extern __shared__ __align__(16) unsigned char ring[];
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int t = s_item;
+        __syncthreads();
+        if (t >= nitems) break;
+        const int4 it = items[t];
+        substage32_tile<SW>(args[it.x], it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
+        __syncthreads();
+    }
+}
+
 // BCON (3dmhdsub.h:720-873) on the FP32 wall planes, evaluated in FP64 from
 // the reconstructed fields, plus the periodic ghost images.
 template <class SW>
-__global__ void k_bcon_ghost32(Grid g, Consts c, Fields8f U, Fields8 Z, const double* bgR, const double* bgT,
-                               double timt) {
-    const int nPx = g.nx - 2, nPy = g.ny - 2;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * nPx * nPy) return;
-    const int wall = t / (nPx * nPy);
-    const int r = t % (nPx * nPy);
-    const int x = 1 + r % nPx, y = 1 + r / nPx;
+__device__ __forceinline__ void bcon32_cell(const Grid& g, const Consts& c, const Fields8f& U, const Fields8& Z,
+                                            const double* bgR, const double* bgT, double timt, int wall, int x, int y) {
     const long long sz = g.sz;
     const int z = wall == 0 ? 1 : g.nz - 2;
     const int s = wall == 0 ? 1 : -1;
@@ -377,6 +398,28 @@ __global__ void k_bcon_ghost32(Grid g, Consts c, Fields8f U, Fields8 Z, const do
             Z.p[S_BZ][i] = 0.0;
         }
     }
+}
+
+template <class SW>
+__global__ void k_bcon_ghost32(Grid g, Consts c, Fields8f U, Fields8 Z, const double* bgR, const double* bgT,
+                               double timt) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nPx * nPy) return;
+    const int r = t % (nPx * nPy);
+    bcon32_cell<SW>(g, c, U, Z, bgR, bgT, timt, t / (nPx * nPy), 1 + r % nPx, 1 + r / nPx);
+}
+
+// BCON for a ragged batch: block b covers 128 wall cells of instance items[b].x from cell items[b].y
+template <class SW>
+__global__ void k_bcon_ghost32_batch(const Fused32Args* __restrict__ args, const int2* __restrict__ items) {
+    const int2 it = items[blockIdx.x];
+    const Fused32Args& a = args[it.x];
+    const int nPx = a.g.nx - 2, nPy = a.g.ny - 2;
+    const int t = it.y + threadIdx.x;
+    if (t >= 2 * nPx * nPy) return;
+    const int r = t % (nPx * nPy);
+    bcon32_cell<SW>(a.g, a.c, a.Uo, a.Z, a.bgR, a.bgT, a.timt, t / (nPx * nPy), 1 + r % nPx, 1 + r / nPx);
 }
 
 // periodic ghost fill of FP32 fields (communicate(), 3dmhdmpi.h:11-143)
@@ -449,7 +492,44 @@ void launch_bcon32(const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const 
     k_bcon_ghost32<SW><<<(n + 127) / 128, 128, 0, st>>>(g, c, U, Z, bgR, bgT, timt);
 }
 
+template <class SW>
+void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, int grid, cudaStream_t st,
+                    int* rc) {
+    k_substage32_batch<SW><<<grid, kThreads, 3 * plane_bytes<SW>(), st>>>(args, items, nitems, counter);
+    *rc = (int)cudaGetLastError();
+}
+
+template <class SW>
+void batch32_occupancy(int* blocks, int* rc) {
+    const size_t smem = 3 * plane_bytes<SW>();
+    cudaFuncSetAttribute(k_substage32_batch<SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    *rc = (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_substage32_batch<SW>, kThreads, smem);
+}
+
+template <class SW>
+void batch32_bcon(const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st) {
+    k_bcon_ghost32_batch<SW><<<nblocks, 128, 0, st>>>(args, items);
+}
+
 }  // namespace
+
+int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter, int grid,
+                           cudaStream_t st) {
+    int rc = 0;
+    MHD_DISPATCH_SW(sw, batch32_launch, args, items, nitems, counter, grid, st, &rc);
+    return rc;
+}
+
+int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm) {
+    int rc = 0;
+    MHD_DISPATCH_SW(sw, batch32_occupancy, blocks_per_sm, &rc);
+    return rc;
+}
+
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st) {
+    MHD_DISPATCH_SW(sw, batch32_bcon, args, items, nblocks, st);
+    return (int)cudaGetLastError();
+}
 
 int fused32_substage(unsigned sw, const Fused32Args& a, cudaStream_t st) {
     int rc = 0;

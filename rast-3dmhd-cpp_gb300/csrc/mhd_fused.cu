@@ -13,10 +13,15 @@ namespace mhd {
 namespace {
 
 using namespace fused;
-using DefaultTile = Tile<32, 4>;
+// tile height of the single-instance kernel (32 x MHD_FUSED_TILE_Y threads)
+#ifndef MHD_FUSED_TILE_Y
+#define MHD_FUSED_TILE_Y 4
+#endif
+using DefaultTile = Tile<32, MHD_FUSED_TILE_Y>;
+constexpr int kMinBlocks = DefaultTile::kThreads >= 256 ? 2 : 3;
 
 template <class SW, bool UXY>
-__global__ void __launch_bounds__(DefaultTile::kThreads) k_substage(FusedArgs a) {
+__global__ void __launch_bounds__(DefaultTile::kThreads, kMinBlocks) k_substage(FusedArgs a) {
     extern __shared__ double ring[];
     const int nPz = a.g.nz - 2;
     const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);

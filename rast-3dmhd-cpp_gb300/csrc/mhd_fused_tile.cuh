@@ -155,6 +155,11 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
     const double c13ore = c.C13 * c.ORE;
     const double kxy = c13ore * cx1 * cy1;
     const double kx13 = c13ore * cx1, ky13 = c13ore * cy1;
+    // RK coefficients: from the host, or from the device time-step record; a
+    // halted record (dt below 1e-8) turns the substage into a copy of U
+    const double gdt = a.dtp ? a.gam * a.dtp[0] : a.gdt;
+    const double zdt = a.dtp ? a.zet * a.dtp[0] : a.zdt;
+    const bool halted = a.dtp && a.dtp[3] != 0.0;
     const double ocvore = c.OCV * c.ORE;
     const double ohm = c.OBETA * c.ORM * c.OCV;
 
@@ -333,11 +338,13 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
 #pragma unroll
             for (int f = 0; f < nf; f++) {
                 const double zf = (a.substage == 0) ? C0(ring_of[f]) : a.Z.p[f][i];
-                const double un = fma(a.gdt, fl[f], zf);
+                const double un = halted ? C0(ring_of[f]) : fma(gdt, fl[f], zf);
                 store_with_images(a.Uo.p[f], g, z, y, x, un);
-                if (a.substage < 2) a.Z.p[f][i] = fma(a.zdt, fl[f], un);
+                if (a.substage < 2) a.Z.p[f][i] = halted ? un : fma(zdt, fl[f], un);
             }
-            if constexpr (SW::lShr) a.FT[i] = ft;
+            if constexpr (SW::lShr) {
+                if (!halted) a.FT[i] = ft;
+            }
         }
         __syncthreads();
         if (z + 2 <= ze) load_plane<SW, T>(a, ring, (z + 2) % 3, z + 2, x0, y0);

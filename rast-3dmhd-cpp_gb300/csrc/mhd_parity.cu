@@ -508,9 +508,12 @@ __global__ void k_cfl(Grid g, Consts c, Fields8 U, double* part) {
         for (int k = 0; k < 5; k++) part[(long long)k * gridDim.x + blockIdx.x] = s[k][0];
 }
 
-__global__ void k_cfl_finish(const double* part, int nb, double* out) {
+// Reduce the per-block CFL partials (5 x nb) into v[0] = max UMACH^2
+// candidate, v[1..4] = min time-step candidates, in thread 0.
+__device__ void reduce_cfl_partials(const double* part, int nb, double v[5]) {
     __shared__ double s[5][256];
-    double v[5] = {0.0, 1e99, 1e99, 1e99, 1e99};
+    v[0] = 0.0;
+    for (int k = 1; k < 5; k++) v[k] = 1e99;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const double a = part[b];
         v[0] = (v[0] < a) ? a : v[0];
@@ -532,8 +535,39 @@ __global__ void k_cfl_finish(const double* part, int nb, double* out) {
         }
         __syncthreads();
     }
+    for (int k = 0; k < 5; k++) v[k] = s[k][0];
+}
+
+__global__ void k_cfl_finish(const double* part, int nb, double* out) {
+    double v[5];
+    reduce_cfl_partials(part, nb, v);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 5; k++) out[k] = s[k][0];
+        for (int k = 0; k < 5; k++) out[k] = v[k];
+}
+
+// DT = SFF * min(candidates) as step() forms it (3dmhdsub.h:44,102-104), kept
+// in the device record; a DT below 1e-8 (or not a number) halts the run as
+// 3dmhd.cpp:292 does: the flag stays set, the record's DT becomes 0 and the
+// substage kernels then leave the state unchanged.  TIMC and TIMT advance as
+// 3dmhdsub.h:150-152 does once per completed step.
+__global__ void k_cfl_record(const double* part, int nb, double sff, int mag, double* rec) {
+    double v[5];
+    reduce_cfl_partials(part, nb, v);
+    if (threadIdx.x != 0) return;
+    auto mn = [](double a, double b) { return (b < a) ? b : a; };
+    const double dt = mag ? sff * mn(mn(v[1], v[2]), mn(v[3], v[4])) : sff * mn(mn(v[1], v[2]), v[3]);
+    const bool stop = rec[3] != 0.0 || !(dt >= 1.0e-8f);
+    if (rec[3] == 0.0) {
+        rec[4] = dt;
+        rec[2] = sqrt(v[0]);
+    }
+    rec[3] = stop ? 1.0 : 0.0;
+    rec[0] = stop ? 0.0 : dt;
+    if (!stop) {
+        rec[7] += dt;
+        rec[1] = rec[6] + rec[7];
+        rec[5] += 1.0;
+    }
 }
 
 int grid_for(long long n, int threads, int cap) {
@@ -600,6 +634,16 @@ int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* part
     if (mag) k_cfl<true><<<nb, 256, 0, st>>>(g, c, U, partials);
     else k_cfl<false><<<nb, 256, 0, st>>>(g, c, U, partials);
     k_cfl_finish<<<1, 256, 0, st>>>(partials, nb, out5);
+    return (int)cudaGetLastError();
+}
+
+int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+                     double* rec, cudaStream_t st) {
+    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
+    const int nb = grid_for(ncell, 256, max_blocks);
+    if (mag) k_cfl<true><<<nb, 256, 0, st>>>(g, c, U, partials);
+    else k_cfl<false><<<nb, 256, 0, st>>>(g, c, U, partials);
+    k_cfl_record<<<1, 256, 0, st>>>(partials, nb, c.SFF, mag ? 1 : 0, rec);
     return (int)cudaGetLastError();
 }
 

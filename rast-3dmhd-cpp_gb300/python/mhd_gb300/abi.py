@@ -13,6 +13,7 @@ PKG = Path(__file__).resolve().parent.parent.parent   # rast-3dmhd-cpp_gb300/
 LIB_PATH = PKG / "lib" / "libmhd_gb300.so"
 
 MHD_OK = 0
+MHD_ERR_NUMERIC, MHD_ERR_DT_TOO_SMALL = -4, -5
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported configuration", -3: "CUDA error",
           -4: "non-finite or non-positive state", -5: "DT too small", -6: "out of device memory",
           -7: "device wait timed out"}
@@ -100,6 +101,7 @@ SIGNATURES = {
     "mhd_cfl_dt": [C.c_void_p, _DP, _DP],
     "mhd_step": [C.c_void_p, C.c_double, C.POINTER(MhdDiag)],
     "mhd_steps": [C.c_void_p, C.c_int, C.c_double],
+    "mhd_steps_cfl": [C.c_void_p, C.c_int, C.POINTER(MhdDiag)],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],
     "mhd_batch_create": [C.POINTER(C.c_void_p), _DP, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)],
@@ -129,7 +131,7 @@ def load(path: Path | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("MHD_GB300_LIB", LIB_PATH))
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
     L = C.CDLL(str(p))

@@ -3,10 +3,10 @@
 Requests (a grid, a step count, a precision, a seed) arrive over time.  The
 server admits a waiting request as soon as its device memory fits in the HBM
 budget next to the simulations already resident, uploads its initial state,
-and steps every resident simulation together: FP64 simulations with the same
-switch set form one ragged batch (one persistent launch per RK3 substage over
-all of their tiles, each step a CUDA graph), FP32-storage simulations run on
-their own streams, so their kernels overlap with the batch.  A simulation
+and steps every resident simulation together: simulations with the same
+precision and switch set form one ragged batch (one persistent launch per RK3
+substage over all of their tiles, each step a CUDA graph); the FP64 and the
+FP32-storage batches run on their own streams, so their kernels overlap.  A simulation
 leaves when its step count is reached; its memory is freed at once and the
 next waiting request takes the slot.  Each step of each simulation computes
 exactly what it would compute alone (the per-cell arithmetic does not depend
@@ -143,9 +143,8 @@ class Server:
     def _groups(self):
         g = {}
         for rid, r in self.resident.items():
-            if r.req.precision == "fp64":
-                key = (r.req.case.lMag, r.req.case.lRot, r.req.case.lShr)
-                g.setdefault(key, []).append(rid)
+            key = (r.req.precision, r.req.case.lMag, r.req.case.lRot, r.req.case.lShr)
+            g.setdefault(key, []).append(rid)
         return g
 
     def _sync_batches(self) -> None:
@@ -158,9 +157,12 @@ class Server:
         for key, rids in groups.items():
             if key not in self.batches:
                 b = Batch([self.resident[r].sim for r in rids])
-                if self.tile is None:
-                    self.tile, _ = b.autotune(report=False)
-                b.set_tile(self.tile)
+                if key[0] == "fp64":
+                    if self.tile is None:
+                        self.tile, _ = b.autotune(report=False)
+                    b.set_tile(self.tile)
+                else:
+                    b.set_tile(0)
                 self.batches[key] = b
                 self.batch_members[key] = list(rids)
                 self.batch_rebuilds += 1
@@ -175,16 +177,10 @@ class Server:
         for key, b in self.batches.items():
             b.steps(q)
         for r in self.resident.values():
-            if r.req.precision != "fp64":
-                r.sim.steps(q, r.req.case.dt)
-        for r in self.resident.values():
             r.remaining -= q
             self.cell_steps += r.req.case.cells * q
         for b in self.batches.values():
             b.sync()
-        for r in self.resident.values():
-            if r.req.precision != "fp64":
-                r.sim.sync()
         return q
 
     def run(self, requests: list, realtime: bool = True, virtual_step_s: float = 1e-3) -> dict:

@@ -151,6 +151,18 @@ class Simulation:
     def steps(self, n: int, dt: float | None = None) -> None:
         self._ck(self.L.mhd_steps(self.ctx, n, self.case.dt if dt is None else dt))
 
+    def steps_cfl(self, n: int, check: bool = True) -> tuple[int, dict]:
+        """n steps with the CFL dt of each (the reference's run mode).
+        Returns (status, diag); status MHD_ERR_DT_TOO_SMALL is the halt of
+        3dmhd.cpp:292 and raises only when check is set."""
+        d = abi.MhdDiag()
+        st = self.L.mhd_steps_cfl(self.ctx, n, C.byref(d))
+        if st in (abi.MHD_OK, abi.MHD_ERR_DT_TOO_SMALL):
+            self.timt = d.timt
+        if check:
+            self._ck(st)
+        return st, d.as_dict()
+
     # ---- timing on the context's stream -------------------------------------
     def timer_start(self) -> None:
         self._ck(self.L.mhd_timer_start(self.ctx))

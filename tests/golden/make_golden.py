@@ -32,7 +32,7 @@ sys.path.insert(0, str(REPO / "oracle"))
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
 
 import refcase  # noqa: E402
-from mhd_gb300.case import FLUX_FIELDS, STATE_FIELDS, config0, initial_state, metrics, small_cases  # noqa: E402
+from mhd_gb300.case import FLUX_FIELDS, STATE_FIELDS, config0, config1, initial_state, metrics, small_cases  # noqa: E402
 
 METRIC_NAMES = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
 CFL_CASES = ("mhd_fixedT", "hydro_default_bc")
@@ -92,6 +92,21 @@ def main() -> None:
     }
     (HERE / "config0_digest.json").write_text(json.dumps(digest, indent=1, sort_keys=True))
     print("wrote config0_digest.json")
+
+    # the 512x512x256 benchmark's physics (lMag, lRot 0.1 about z, lShr) at 64x64x32, 20 steps
+    c1 = config1().replace(nPx=64, nPy=64, nPz=32, nPEy=2, nPEz=2, name="config1_physics_64x64x32")
+    st = initial_state(c1)
+    r = refcase.run(c1, st, "steps", 20)
+    digest = {
+        "case": c1.to_dict(),
+        "steps": 20,
+        "reference_ranks": 4,
+        "input_sha256": {k: sha(st[k]) for k in STATE_FIELDS},
+        "output_sha256": {k: sha(r[k]) for k in STATE_FIELDS},
+        "output_interior_absmax": {k: float(np.abs(r[k][1:-1, 1:-1, 1:-1]).max()) for k in STATE_FIELDS},
+    }
+    (HERE / "config1_64x64x32_digest.json").write_text(json.dumps(digest, indent=1, sort_keys=True))
+    print("wrote config1_64x64x32_digest.json")
 
 
 if __name__ == "__main__":

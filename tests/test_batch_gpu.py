@@ -107,3 +107,36 @@ def test_mixed_switch_sets_rejected():
         Batch([a, c])
     a.close()
     c.close()
+
+
+def test_fp32_batch_equals_instances_alone():
+    cases = make_cases(seed0=60)[:4]
+
+    def fresh32(c):
+        s = Simulation(c, precision="fp32")
+        s.upload_state(initial_state(c))
+        s.communicate()
+        return s
+    sims = [fresh32(c) for c in cases]
+    b = Batch(sims)
+    b.steps(3)
+    b.sync()
+    got = [s.download_state() for s in sims]
+    b.close()
+    for s in sims:
+        s.close()
+    for i, c in enumerate(cases):
+        solo = fresh32(c)
+        bs = Batch([solo])
+        bs.steps(3)
+        bs.sync()
+        ref = solo.download_state()
+        bs.close()
+        solo.close()
+        plain = fresh32(c)
+        plain.steps(3, c.dt)
+        pl = plain.download_state()
+        plain.close()
+        for k in STATE_FIELDS:
+            assert np.array_equal(got[i][k], ref[k]), (i, k)
+            assert rel_err(got[i][k], pl[k]) <= 1e-6, (i, k)

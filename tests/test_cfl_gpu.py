@@ -1,0 +1,111 @@
+"""The reference's run mode, a CFL dt for every step (step(),
+3dmhdsub.h:36-106, in the loop of 3dmhd.cpp:271-331), through
+mhd_steps_cfl.  On the fused FP64 path the dt is reduced into a
+device-resident record that the substage kernels read, so n steps run
+without a host round trip; the parity and FP32-storage paths read dt back
+each step.  A dt below 1e-8 halts the run (3dmhd.cpp:292)."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_util import rel_err, sim_from_fixture
+from mhd_gb300 import abi
+from mhd_gb300.case import STATE_FIELDS, Case, initial_state
+from mhd_gb300.sim import Simulation
+
+pytestmark = pytest.mark.gpu
+TOL_ONE_STEP = 1e-12
+
+
+@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc"])
+def test_parity_path_steps_cfl_bit_exact_vs_reference(name):
+    case, g = load_golden(name)
+    sim = sim_from_fixture(case, g, "parity")
+    st, d = sim.steps_cfl(2)
+    assert st == abi.MHD_OK and d["nit"] == 2
+    assert d["dt"] == g["cfl2_dt"][1]
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(sim.download(k), g["cfl2_" + k]), k
+    sim.close()
+
+
+@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc"])
+def test_fused_device_dt_vs_reference(name):
+    """The first dt comes from the reference's own initial state, so it is
+    bit-exact; the second is reduced over the fused state (1e-12 of the
+    reference's), and the state after two steps agrees to 1e-12 per field."""
+    case, g = load_golden(name)
+    sim = sim_from_fixture(case, g, "fused")
+    _, d1 = sim.steps_cfl(1)
+    assert d1["dt"] == g["cfl2_dt"][0]
+    _, d2 = sim.steps_cfl(1)
+    assert abs(d2["dt"] - g["cfl2_dt"][1]) <= TOL_ONE_STEP * g["cfl2_dt"][1]
+    # TIMT = TIMI + TIMC with TIMC the running sum of DT (3dmhdsub.h:150-152)
+    assert d2["timt"] == 0.0 + (d1["dt"] + d2["dt"]) and d2["nit"] == 2
+    for k in STATE_FIELDS[:case.nfields]:
+        assert rel_err(sim.download(k), g["cfl2_" + k]) <= 2 * TOL_ONE_STEP, k
+    sim.close()
+
+
+@pytest.mark.parametrize("lmag,lshr", [(True, True), (False, False)])
+def test_device_record_equals_host_cfl_steps(lmag, lshr):
+    """20 steps with the dt kept on the device equal, bit for bit, 20 steps
+    whose CFL dt went through the host (same reductions, same kernels)."""
+    case = Case(nPx=40, nPy=48, nPz=24, lMag=lmag, lRot=True, lShr=lshr, seed=5, name="cfl")
+    st0 = initial_state(case)
+    a, b = Simulation(case), Simulation(case)
+    for s in (a, b):
+        s.upload_state(st0)
+        s.communicate()
+    _, da = a.steps_cfl(20)
+    for _ in range(20):
+        db = b.step(0.0)
+    assert da["dt"] == db["dt"] and da["timt"] == db["timt"] and da["nit"] == db["nit"] == 20
+    assert da["umach"] == db["umach"]
+    ga, gb = a.download_state(), b.download_state()
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(ga[k], gb[k]), k
+    a.close()
+    b.close()
+
+
+def test_halt_leaves_state_unchanged():
+    """SFF = 1e-12 makes every CFL dt fall below 1e-8: after one fixed-dt
+    step the halted steps leave the state as it was, bit for bit, and report
+    MHD_ERR_DT_TOO_SMALL with nit and timt of the last completed step."""
+    case = Case(nPx=32, nPy=32, nPz=16, lMag=True, seed=9, SFF=1e-12, name="halt")
+    sim = Simulation(case)
+    sim.upload_state(initial_state(case))
+    sim.communicate()
+    sim.step(case.dt)
+    before = sim.download_state()
+    st, d = sim.steps_cfl(5, check=False)
+    assert st == abi.MHD_ERR_DT_TOO_SMALL
+    assert d["nit"] == 1 and d["timt"] == case.dt and 0.0 < d["dt"] < 1e-8
+    after = sim.download_state()
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(before[k], after[k]), k
+    # the host-side CFL step halts the same way
+    with pytest.raises(abi.MhdError):
+        sim.step(0.0)
+    # and a fixed-dt step still runs afterwards
+    sim.step(case.dt)
+    assert sim.diagnostics()["nit"] == 2
+    sim.close()
+
+
+def test_fp32_storage_steps_cfl():
+    """The FP32-storage form takes the CFL dt from its FP64 reduction; its
+    first dt equals the FP64 one to the FP32 storage rounding."""
+    case = Case(nPx=32, nPy=32, nPz=32, lMag=True, seed=3, name="cfl32")
+    st0 = initial_state(case)
+    s64, s32 = Simulation(case), Simulation(case, precision="fp32")
+    for s in (s64, s32):
+        s.upload_state(st0)
+        s.communicate()
+    _, d64 = s64.steps_cfl(3)
+    _, d32 = s32.steps_cfl(3)
+    assert d32["nit"] == 3
+    assert abs(d32["dt"] - d64["dt"]) <= 1e-5 * d64["dt"]
+    s64.close()
+    s32.close()

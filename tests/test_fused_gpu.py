@@ -129,3 +129,36 @@ def test_device_initial_state_matches_host_mirror():
     t1 = 1.0 + case.THETA * z_coordinate(case)
     g = (want["TT"][1:-1, 1:-1, 1:-1] / t1[1:-1, None, None] - 1) / case.noise
     assert abs(g.mean()) < 0.2 and 0.8 < g.std() < 1.2
+
+
+def test_config1_full_size_one_step(capsys):
+    """512x512x256 with lMag, lRot and lShr: one fused step against the
+    oracle on every cell (the 64x64x32 sub-blocks and the rest)."""
+    from mhd_gb300.case import config1
+    case = config1()
+    st = initial_state(case)
+    sim = Simulation(case, path="fused")
+    sim.upload_state(st)
+    sim.communicate()
+    sim.step(case.dt)
+    got = sim.download_state()
+    sim.close()
+    o = oracle_for(case, st, nthreads=16)
+    o.steps(1)
+    errs = {k: rel_err(got[k], o.arr[k]) for k in STATE_FIELDS}
+    # 64x64x32 sub-blocks, as the configuration asks: the worst block per field
+    worst = {}
+    for k in STATE_FIELDS:
+        ref = o.arr[k]
+        scale = np.abs(ref[1:-1]).max()
+        w = 0.0
+        for z0 in range(1, case.nz - 1, 32):
+            for y0 in range(1, case.ny - 1, 64):
+                for x0 in range(1, case.nx - 1, 64):
+                    sl = np.s_[z0:z0 + 32, y0:y0 + 64, x0:x0 + 64]
+                    w = max(w, np.abs(got[k][sl] - ref[sl]).max() / scale)
+        worst[k] = w
+    with capsys.disabled():
+        print("\n512x512x256 one fused step vs oracle, worst 64x64x32 block:", {k: f"{v:.1e}" for k, v in worst.items()})
+    for k in STATE_FIELDS:
+        assert errs[k] <= TOL_ONE_STEP and worst[k] <= TOL_ONE_STEP, k

@@ -110,3 +110,19 @@ def test_dat0_writer_matches_reference_dump(name, tmp_path):
                            back.ctypes.data_as(C.POINTER(C.c_double)), case.nPEy, case.nPEz, 0) == 0
     I = np.s_[:, 1:-1, 1:-1, 1:-1]
     assert np.array_equal(back[I], state[I])
+
+
+def test_config1_physics_64x64x32_20_steps_digest():
+    """lMag + lRot (0.1 about z) + lShr at 64x64x32: the oracle's state after
+    20 steps hashes to the reference's (4 ranks)."""
+    from mhd_gb300.case import config1
+    d = json.loads((GOLDEN / "config1_64x64x32_digest.json").read_text())
+    case = config1().replace(nPx=64, nPy=64, nPz=32, nPEy=2, nPEz=2, name="config1_physics_64x64x32")
+    st = initial_state(case)
+    if any(_sha(st[k]) != d["input_sha256"][k] for k in STATE_FIELDS):
+        pytest.skip("this host's libm generates a different seeded input; digest not comparable")
+    sim = oracle.OracleSim(case, st, nthreads=8)
+    sim.communicate()
+    sim.steps(d["steps"])
+    for k in STATE_FIELDS:
+        assert _sha(sim.arr[k]) == d["output_sha256"][k], k

@@ -76,3 +76,21 @@ def test_config0_parity_100_steps_bit_exact():
     for k in STATE_FIELDS:
         assert np.array_equal(sim.download(k), o.arr[k]), k
     sim.close()
+
+
+def test_config1_physics_parity_20_steps_bit_exact():
+    """The benchmark's physics (lMag, lRot 0.1 about z, lShr) at 64x64x32:
+    20 steps through the unfused GPU path equal the oracle (whose digest
+    equals the reference's) bit for bit."""
+    from mhd_gb300.case import config1
+    case = config1().replace(nPx=64, nPy=64, nPz=32, nPEy=2, nPEz=2)
+    st = initial_state(case)
+    sim = Simulation(case, path="parity")
+    sim.upload_state(st)
+    sim.communicate()
+    sim.steps(20, case.dt)
+    o = oracle_for(case, st, nthreads=16)
+    o.steps(20)
+    for k in STATE_FIELDS:
+        assert np.array_equal(sim.download(k), o.arr[k]), k
+    sim.close()
