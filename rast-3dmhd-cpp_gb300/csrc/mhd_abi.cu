@@ -498,6 +498,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     c.GRAV = p.GRAV; c.THETA = p.THETA; c.RE = p.RE; c.REPR = ctx->k.REPR; c.ORE = ctx->k.ORE;
     c.OCV = ctx->k.OCV; c.CV = ctx->k.CV; c.GAMMA = p.GAMMA; c.OMX = ctx->k.OMX; c.OMZ = ctx->k.OMZ;
     c.RM = p.RM; c.ORM = ctx->k.ORM; c.OBETA = ctx->k.OBETA; c.TB = p.TB; c.TP = p.TP; c.SFF = p.SFF;
+    c.DDXmin = HUGE_VAL;
+    for (int x = 1; x <= nx - 2; x++) c.DDXmin = (p.DDX[x] < c.DDXmin) ? p.DDX[x] : c.DDXmin;
     c.izCon = p.izCon; c.iTCon = p.iTCon; c.iBCon = p.iBCon;
 
     ctx->red_blocks = 152 * 8;

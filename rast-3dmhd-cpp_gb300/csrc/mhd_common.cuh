@@ -43,6 +43,7 @@ struct Consts {
     double C13, C23, C43;
     double hx, h2x, hy, h2y, hz, h2z;
     double GRAV, THETA, RE, REPR, ORE, OCV, CV, GAMMA, OMX, OMZ, RM, ORM, OBETA, TB, TP, SFF;
+    double DDXmin;  // min of DDX over interior x (NaN skipped), for the CFL reduction
     int izCon, iTCon, iBCon, pad_;
     const double *dxxdx, *d2xxdx2, *DDX;
     const double *dyydy, *d2yydy2, *DDY;

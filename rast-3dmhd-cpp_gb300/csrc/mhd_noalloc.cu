@@ -109,6 +109,7 @@ extern "C" int mhd_fluxes_noalloc(const mhd_fluxes_noalloc_args* a, void* stream
     c.GRAV = a->GRAV; c.THETA = a->THETA; c.RE = a->RE; c.REPR = k.REPR; c.ORE = k.ORE; c.OCV = k.OCV; c.CV = k.CV;
     c.GAMMA = a->GAMMA; c.OMX = k.OMX; c.OMZ = k.OMZ; c.RM = a->RM; c.ORM = k.ORM; c.OBETA = k.OBETA;
     c.TB = a->TB; c.TP = a->TP; c.SFF = a->SFF;
+    c.DDXmin = -HUGE_VAL;  // no CFL reduction here
     c.izCon = a->izCon; c.iTCon = a->iTCon; c.iBCon = a->iBCon;
     c.dxxdx = a->dxxdx; c.d2xxdx2 = a->d2xxdx2; c.DDX = a->DDX;
     c.dyydy = a->dyydy; c.d2yydy2 = a->d2yydy2; c.DDY = a->DDY;

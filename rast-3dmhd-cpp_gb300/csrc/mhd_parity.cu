@@ -448,44 +448,65 @@ __global__ void k_comm(int nf, Grid g, Fields8 U) {
     }
 }
 
-// CFL candidates of step() (3dmhdsub.h:36-106), reduced per block; min/max
-// are exact, so the block order does not change the result.
+// ---- CFL time step of step() (3dmhdsub.h:36-106) ---------------------------
+// Per cell: UMACH^2 candidate mc = OGAMMA*UU/T, and four time-step candidates
+// a0 = DD/sqrt(UU') (fast mode), a1 (conduction), a2 (viscosity), a3
+// (resistivity), with DD the smallest grid spacing at the cell.  The helpers
+// keep the reference's expressions and association (this file is compiled
+// without FMA contraction), so every candidate is bit-exact.
+
+__device__ __forceinline__ double cfl_dd_yz(const Consts& c, int y, int z) {
+    return (c.DDZ[z] < c.DDY[y]) ? c.DDZ[z] : c.DDY[y];
+}
+__device__ __forceinline__ double cfl_a1(const Consts& c, double DD, double ro, int z) {
+    return 0.5f * DD * DD * c.REPR * c.CV * ro / c.RKAPA[z];
+}
+__device__ __forceinline__ double cfl_a2(const Consts& c, double DD, double ro) { return 0.375f * DD * DD * c.RE * ro; }
+__device__ __forceinline__ double cfl_a3(const Consts& c, double DD) { return 0.5f * DD * DD * c.RM; }
+
+// mc and the fast-mode speed^2 UU' of cell i
 template <bool MAG>
-__global__ void k_cfl(Grid g, Consts c, Fields8 U, double* part) {
-    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
-    const long long ncell = (long long)nPx * nPy * nPz;
-    const double OGAMMA = 1.0f / c.GAMMA;
-    double um = 0.0f, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int x = 1 + (int)(t % nPx);
-        const int y = 1 + (int)((t / nPx) % nPy);
-        const int z = 1 + (int)(t / ((long long)nPx * nPy));
-        const long long i = z * g.sz + y * g.sy + x;
-        const double ru = U.p[S_RU][i], rv = U.p[S_RV][i], rw = U.p[S_RW][i], ro = U.p[S_RO][i], tt = U.p[S_TT][i];
-        double UU = (ru * ru + rv * rv + rw * rw) / (ro * ro);
-        const double mc = OGAMMA * UU / tt;
-        um = (um < mc) ? mc : um;
-        if constexpr (MAG) {
-            const double bx = U.p[S_BX][i], by = U.p[S_BY][i], bz = U.p[S_BZ][i];
-            UU += c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro +
-                  2.0f * sqrt(UU * (c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro));
-        } else {
-            UU += c.GAMMA * tt + 2.0f * sqrt(c.GAMMA * UU * tt);
-        }
-        double DD = (c.DDZ[z] < c.DDY[y]) ? c.DDZ[z] : c.DDY[y];
-        if (g.nx > 3) DD = (c.DDX[x] < DD) ? c.DDX[x] : DD;
-        const double a0 = DD / sqrt(UU);
-        const double a1 = 0.5f * DD * DD * c.REPR * c.CV * ro / c.RKAPA[z];
-        const double a2 = 0.375f * DD * DD * c.RE * ro;
-        w0 = (a0 < w0) ? a0 : w0;
-        w1 = (a1 < w1) ? a1 : w1;
-        w2 = (a2 < w2) ? a2 : w2;
-        if constexpr (MAG) {
-            const double a3 = 0.5f * DD * DD * c.RM;
-            w3 = (a3 < w3) ? a3 : w3;
-        }
+__device__ __forceinline__ void cfl_speeds(const Consts& c, const Fields8& U, long long i, double OGAMMA, double& mc,
+                                           double& uu) {
+    const double ru = U.p[S_RU][i], rv = U.p[S_RV][i], rw = U.p[S_RW][i], ro = U.p[S_RO][i], tt = U.p[S_TT][i];
+    double UU = (ru * ru + rv * rv + rw * rw) / (ro * ro);
+    mc = OGAMMA * UU / tt;
+    if constexpr (MAG) {
+        const double bx = U.p[S_BX][i], by = U.p[S_BY][i], bz = U.p[S_BZ][i];
+        UU += c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro +
+              2.0f * sqrt(UU * (c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro));
+    } else {
+        UU += c.GAMMA * tt + 2.0f * sqrt(c.GAMMA * UU * tt);
     }
+    uu = UU;
+}
+
+// all five candidates of cell (x, y, z), folded into the running extrema
+template <bool MAG>
+__device__ __forceinline__ void cfl_cell(const Grid& g, const Consts& c, const Fields8& U, int x, int y, int z,
+                                         double OGAMMA, double& um, double& w0, double& w1, double& w2, double& w3) {
+    const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
+    double mc, UU;
+    cfl_speeds<MAG>(c, U, i, OGAMMA, mc, UU);
+    um = (um < mc) ? mc : um;
+    double DD = cfl_dd_yz(c, y, z);
+    if (g.nx > 3) DD = (c.DDX[x] < DD) ? c.DDX[x] : DD;
+    const double ro = U.p[S_RO][i];
+    const double a0 = DD / sqrt(UU);
+    const double a1 = cfl_a1(c, DD, ro, z);
+    const double a2 = cfl_a2(c, DD, ro);
+    w0 = (a0 < w0) ? a0 : w0;
+    w1 = (a1 < w1) ? a1 : w1;
+    w2 = (a2 < w2) ? a2 : w2;
+    if constexpr (MAG) {
+        const double a3 = cfl_a3(c, DD);
+        w3 = (a3 < w3) ? a3 : w3;
+    }
+}
+
+// Block reduction of the running extrema into partials [5][gridDim.x]
+// (blockDim.x = 256); min/max are exact, so no order changes the result.
+__device__ void write_cfl_partials(double um, double w0, double w1, double w2, double w3, double* part) {
     __shared__ double s[5][256];
     s[0][threadIdx.x] = um;
     s[1][threadIdx.x] = w0;
@@ -506,6 +527,166 @@ __global__ void k_cfl(Grid g, Consts c, Fields8 U, double* part) {
     }
     if (threadIdx.x == 0)
         for (int k = 0; k < 5; k++) part[(long long)k * gridDim.x + blockIdx.x] = s[k][0];
+}
+
+// float value of d with its significand truncated to 23 bits (relative error
+// below 2^-23), formed with integer operations only; magnitudes below 2^-126
+// become 0 and magnitudes beyond the float range (and NaN) become infinity.
+__device__ __forceinline__ float trunc_to_f32(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);
+    unsigned b;
+    if (e <= 0) b = sign;
+    else if (e >= 255) b = sign | 0x7f800000u;
+    else b = sign | ((unsigned)e << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
+    return __uint_as_float(b);
+}
+
+__device__ __forceinline__ bool nonzero_bits(double d) {
+    return (((unsigned)__double2hiint(d) & 0x7fffffffu) | (unsigned)__double2loint(d)) != 0u;
+}
+
+constexpr int kCflK = 8;                         // cells per lane in one pass over a row
+constexpr int kCflWarps = 8;                     // 256 threads
+constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x the approximation error
+
+// The CFL reduction, one warp per (y, z) row of cells.
+//
+// On a row whose DD is the same in every cell (DDX never below
+// min(DDZ[z], DDY[y]); always so on uniform x/y grids) the candidates need no
+// per-cell FP64 arithmetic except where they can decide the result:
+//   * a1, a2 are products/quotients of ro with positive row constants and a3
+//     depends on DD alone; rounding is monotone, so their row minima are the
+//     candidates of the row's smallest ro (an exact FP64 min);
+//   * a0 = DD/sqrt(UU') is smallest where UU' is largest; UU' and mc are
+//     estimated in FP32 from inputs truncated to 23 bits (error below 1.2e-6
+//     for inputs in the accepted ranges), the cells whose estimate lies within
+//     2^-16 of the pass's largest are evaluated exactly, and every cell whose
+//     estimate is not certified (out-of-range input, non-finite value) too.
+// The row's exact maximum of mc and minimum of a0 are therefore among the cells
+// evaluated exactly, and the result equals the cell-by-cell reduction bit for
+// bit.  Rows with varying DD, and launches whose constants break the
+// monotonicity (non-positive factors), evaluate every cell exactly.
+template <bool MAG>
+__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, Fields8 U, double* part) {
+    __shared__ int list[kCflWarps][32 * kCflK];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
+    const long long nrows = (long long)nPy * nPz;
+    const double OGAMMA = 1.0f / c.GAMMA;
+    const bool consts_ok = (c.GAMMA >= 0x1p-10 && c.GAMMA <= 0x1p10) && (c.OBETA >= 0.0 && c.OBETA <= 0x1p30);
+    const float gam_f = (float)c.GAMMA, obeta_f = (float)c.OBETA;
+    double um = 0.0f, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
+    for (long long r = (long long)blockIdx.x * kCflWarps + wid; r < nrows; r += (long long)gridDim.x * kCflWarps) {
+        const int y = 1 + (int)(r % nPy), z = 1 + (int)(r / nPy);
+        const long long row = (long long)z * g.sz + (long long)y * g.sy;
+        const double DDyz = cfl_dd_yz(c, y, z);
+        const double P1 = 0.5f * DDyz * DDyz * c.REPR * c.CV;  // prefix of cfl_a1
+        const double P2 = 0.375f * DDyz * DDyz * c.RE;         // prefix of cfl_a2
+        const bool fast = consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 &&
+                          c.RKAPA[z] > 0.0;
+        if (!fast) {
+            for (int x = 1 + lane; x <= nPx; x += 32) cfl_cell<MAG>(g, c, U, x, y, z, OGAMMA, um, w0, w1, w2, w3);
+            continue;
+        }
+        double mro = __longlong_as_double(0x7ff0000000000000LL);  // +inf: no cell yet
+        for (int x0 = 1; x0 <= nPx; x0 += 32 * kCflK) {
+            float uA[kCflK], mA[kCflK];
+            unsigned okm = 0u, nzm = 0u, valid = 0u;
+            float Mu = -INFINITY, Mm = -INFINITY;
+#pragma unroll
+            for (int k = 0; k < kCflK; k++) {
+                const int x = x0 + k * 32 + lane;
+                uA[k] = 0.0f;
+                mA[k] = 0.0f;
+                if (x > nPx) continue;
+                valid |= 1u << k;
+                const long long i = row + x;
+                const double rud = U.p[S_RU][i], rvd = U.p[S_RV][i], rwd = U.p[S_RW][i];
+                const double rod = U.p[S_RO][i], ttd = U.p[S_TT][i];
+                mro = (rod < mro) ? rod : mro;
+                const bool nz = nonzero_bits(rud) || nonzero_bits(rvd) || nonzero_bits(rwd);
+                const float ru = trunc_to_f32(rud), rv = trunc_to_f32(rvd), rw = trunc_to_f32(rwd);
+                const float ro = trunc_to_f32(rod), tt = trunc_to_f32(ttd);
+                const float ir = __frcp_rn(ro);
+                const float sq = __fadd_rn(__fadd_rn(__fmul_rn(ru, ru), __fmul_rn(rv, rv)), __fmul_rn(rw, rw));
+                const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
+                float G = __fmul_rn(gam_f, tt);
+                if constexpr (MAG) {
+                    const float bx = trunc_to_f32(U.p[S_BX][i]), by = trunc_to_f32(U.p[S_BY][i]),
+                                bz = trunc_to_f32(U.p[S_BZ][i]);
+                    const float b2 = __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
+                    G = __fadd_rn(G, __fmul_rn(__fmul_rn(obeta_f, b2), ir));
+                }
+                const float uuf = __fadd_rn(__fadd_rn(uuk, G), __fmul_rn(2.0f, __fsqrt_rn(__fmul_rn(uuk, G))));
+                const float mc = __fdiv_rn(uuk, tt);
+                const bool ok = (ro >= 0x1p-20f && ro <= 0x1p20f) && (tt >= 0x1p-20f && tt <= 0x1p20f) &&
+                                isfinite(uuf) && isfinite(mc);
+                uA[k] = uuf;
+                mA[k] = mc;
+                if (ok) {
+                    okm |= 1u << k;
+                    Mu = fmaxf(Mu, uuf);
+                    if (nz) Mm = fmaxf(Mm, mc);
+                }
+                if (nz) nzm |= 1u << k;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Mu = fmaxf(Mu, __shfl_xor_sync(0xffffffffu, Mu, o));
+                Mm = fmaxf(Mm, __shfl_xor_sync(0xffffffffu, Mm, o));
+            }
+            const float tu = Mu - kCflTau * Mu;
+            const float tm = (Mm >= 0x1p-40f) ? Mm - kCflTau * Mm : -INFINITY;
+            int n = 0;
+#pragma unroll
+            for (int k = 0; k < kCflK; k++) {
+                const bool v = (valid >> k) & 1u, ok = (okm >> k) & 1u, nz = (nzm >> k) & 1u;
+                const bool cand = v && (!ok || uA[k] >= tu || (nz && mA[k] >= tm));
+                const unsigned bal = __ballot_sync(0xffffffffu, cand);
+                if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
+                n += __popc(bal);
+            }
+            __syncwarp();
+            for (int j = lane; j < n; j += 32) {
+                const int x = list[wid][j];
+                double mc, UU;
+                cfl_speeds<MAG>(c, U, row + x, OGAMMA, mc, UU);
+                um = (um < mc) ? mc : um;
+                const double a0 = DDyz / sqrt(UU);
+                w0 = (a0 < w0) ? a0 : w0;
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double q = __shfl_xor_sync(0xffffffffu, mro, o);
+            mro = (q < mro) ? q : mro;
+        }
+        if (lane == 0) {
+            const double a1 = cfl_a1(c, DDyz, mro, z), a2 = cfl_a2(c, DDyz, mro);
+            w1 = (a1 < w1) ? a1 : w1;
+            w2 = (a2 < w2) ? a2 : w2;
+            if constexpr (MAG) {
+                const double a3 = cfl_a3(c, DDyz);
+                w3 = (a3 < w3) ? a3 : w3;
+            }
+        }
+    }
+    write_cfl_partials(um, w0, w1, w2, w3, part);
+}
+
+// Launch the row reduction; returns the number of partial blocks.
+int launch_cfl_rows(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+                    cudaStream_t st) {
+    const long long nrows = (long long)(g.ny - 2) * (g.nz - 2);
+    long long nb = (nrows + kCflWarps - 1) / kCflWarps;
+    if (nb < 1) nb = 1;
+    if (nb > max_blocks) nb = max_blocks;
+    if (mag) k_cfl_rows<true><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, partials);
+    else k_cfl_rows<false><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, partials);
+    return (int)nb;
 }
 
 // Reduce the per-block CFL partials (5 x nb) into v[0] = max UMACH^2
@@ -629,20 +810,14 @@ int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st) {
 
 int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks, double* out5,
                cudaStream_t st) {
-    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
-    const int nb = grid_for(ncell, 256, max_blocks);
-    if (mag) k_cfl<true><<<nb, 256, 0, st>>>(g, c, U, partials);
-    else k_cfl<false><<<nb, 256, 0, st>>>(g, c, U, partials);
+    const int nb = launch_cfl_rows(mag, g, c, U, partials, max_blocks, st);
     k_cfl_finish<<<1, 256, 0, st>>>(partials, nb, out5);
     return (int)cudaGetLastError();
 }
 
 int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
                      double* rec, cudaStream_t st) {
-    const long long ncell = (long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2);
-    const int nb = grid_for(ncell, 256, max_blocks);
-    if (mag) k_cfl<true><<<nb, 256, 0, st>>>(g, c, U, partials);
-    else k_cfl<false><<<nb, 256, 0, st>>>(g, c, U, partials);
+    const int nb = launch_cfl_rows(mag, g, c, U, partials, max_blocks, st);
     k_cfl_record<<<1, 256, 0, st>>>(partials, nb, c.SFF, mag ? 1 : 0, rec);
     return (int)cudaGetLastError();
 }

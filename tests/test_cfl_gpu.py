@@ -10,8 +10,10 @@ import pytest
 from conftest import load_golden
 from gpu_util import rel_err, sim_from_fixture
 from mhd_gb300 import abi
-from mhd_gb300.case import STATE_FIELDS, Case, initial_state
+from mhd_gb300.case import STATE_FIELDS, Case, initial_state, metrics
 from mhd_gb300.sim import Simulation
+
+import oracle
 
 pytestmark = pytest.mark.gpu
 TOL_ONE_STEP = 1e-12
@@ -109,3 +111,90 @@ def test_fp32_storage_steps_cfl():
     assert abs(d32["dt"] - d64["dt"]) <= 1e-5 * d64["dt"]
     s64.close()
     s32.close()
+
+
+# ---- the row-filtered CFL reduction against the oracle, bit for bit ----------
+def _cfl_pair(case, st, ddx=None):
+    mo = {"DDX": ddx} if ddx is not None else None
+    sim = Simulation(case, metric_override=mo)
+    sim.upload_state(st)
+    got = sim.cfl_dt()
+    o = oracle.OracleSim(case, st)
+    if ddx is not None:
+        o._metric_arrays[2][:] = ddx      # the oracle reads DDX through this array
+    want = o.cfl_dt()
+    sim.close()
+    return got, want
+
+
+def _random_flow(case, seed, amp):
+    st = initial_state(case)
+    rng = np.random.default_rng(seed)
+    for k in ("RU", "RV", "RW"):
+        st[k] = amp * rng.standard_normal(case.shape) * st["RO"]
+    if case.lMag:
+        for k in ("BX", "BY", "BZ"):
+            st[k] = 1e-2 * rng.standard_normal(case.shape)
+    return st
+
+
+@pytest.mark.parametrize("lmag", [True, False])
+@pytest.mark.parametrize("kind", ["initial", "flow", "ties", "tiny_and_odd", "nan_cell"])
+def test_cfl_reduction_bit_exact(lmag, kind):
+    """DT and UMACH of mhd_cfl_dt equal the oracle's cell-by-cell reduction
+    (the reference's loop) bit for bit: zero momenta, a random flow, a state
+    where every cell ties, states with tiny, huge, negative and non-finite
+    values (cells the FP32 estimate cannot certify)."""
+    case = Case(nPx=70, nPy=36, nPz=20, lMag=lmag, seed=11, name="cflx")
+    if kind == "initial":
+        st = initial_state(case)
+    elif kind == "flow":
+        st = _random_flow(case, 1, 3e-2)
+    elif kind == "ties":
+        st = initial_state(case)
+        st["TT"][...] = 2.0
+        st["RO"][...] = 0.5
+        st["RU"][...] = 0.01
+        st["RV"][...] = -0.02
+        st["RW"][...] = 0.0
+    elif kind == "tiny_and_odd":
+        st = _random_flow(case, 2, 1e-25)
+        st["RU"][7, 9, 11] = 3e-3                  # one real flow cell
+        st["RV"][5, 20, 40] = 1e30                 # beyond the float range
+        st["TT"][9, 3, 3] = -0.5                   # negative temperature
+        st["RO"][12, 30, 60] = 1e-30               # density far below the certified range
+        st["RW"][3, 4, 5] = 1e-300                 # subnormal-range input
+    else:
+        st = _random_flow(case, 3, 1e-2)
+        st["TT"][6, 6, 6] = np.nan
+        st["RU"][8, 8, 8] = np.nan
+    got, want = _cfl_pair(case, st)
+    assert got[0] == want[0] or (np.isnan(got[0]) and np.isnan(want[0])), (got, want)
+    assert got[1] == want[1] or (np.isnan(got[1]) and np.isnan(want[1])), (got, want)
+
+
+def test_cfl_reduction_varying_dd_rows():
+    """A non-uniform DDX makes DD vary along rows where it drops below
+    min(DDZ, DDY): those rows take the cell-by-cell path; the result stays
+    bit-exact."""
+    case = Case(nPx=64, nPy=24, nPz=16, lMag=True, seed=4, name="cfldd")
+    st = _random_flow(case, 4, 2e-2)
+    base = float(metrics(case).DDX[1])
+    x = np.arange(case.nx)
+    ddx = base * (1.0 + 0.6 * np.sin(0.37 * x))
+    got, want = _cfl_pair(case, st, ddx=ddx)
+    assert got == want
+
+
+def test_cfl_reduction_after_fused_steps():
+    """The reduction over states the fused path produced (the adaptive run)."""
+    case = Case(nPx=96, nPy=64, nPz=32, lMag=True, lRot=True, seed=6, noise=1e-2, name="cflrun")
+    sim = Simulation(case)
+    sim.upload_state(initial_state(case))
+    sim.communicate()
+    sim.steps_cfl(30)
+    st = sim.download_state()
+    got = sim.cfl_dt()
+    sim.close()
+    want = oracle.OracleSim(case, st).cfl_dt()
+    assert got == want
