@@ -219,9 +219,26 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt);
  * (MHD_ERR_NUMERIC for a non-finite dt).  `out` (may be NULL) receives the
  * dt of the last step computed, umach, timt and nit. */
 int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out);
+/* One fixed-dt fused FP64 step from a host state to a host state: `in` is
+ * uploaded and the new state is written to `out` (both nf x nz x ny x nx
+ * doubles, field-major as in mhd_upload_state; they may be the same buffer;
+ * pinned memory (mhd_host_alloc) lets the copies overlap the computation).
+ * The interior is cut into z slabs that are uploaded, stepped and downloaded
+ * as a wavefront on three streams, so the copies hide behind the kernels;
+ * the result is bit-identical to mhd_upload_state + mhd_step +
+ * mhd_download_state.  in = NULL steps the device state; out = NULL skips the
+ * download and the call does not block (then `in` must stay unchanged until
+ * mhd_sync).  Replaces the transfers around step() of a host-resident driver;
+ * the reference has no counterpart (its state never leaves the host). */
+int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double dt);
 /* Mass, energy, max|div B| and sanity flags of the current state (blocks). */
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
 int mhd_sync(mhd_ctx* ctx);
+
+/* Self-check: the integer-pipe float<->double conversions the FP32-storage
+ * kernels use against the hardware conversions, on n test patterns of seed;
+ * *mismatches receives the number of differing results (0 expected). */
+int mhd_selftest_convert(long long n, unsigned long long seed, long long* mismatches);
 
 /* ---- ragged batches ------------------------------------------------------ */
 /* n independent instances (fused-path contexts with one switch set and one

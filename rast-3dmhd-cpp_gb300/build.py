@@ -35,6 +35,8 @@ UNITS = [
     ("mhd_batch.cu", "mhd_batch", []),
     ("mhd_io.cu", "mhd_io", []),
     ("mhd_init.cu", "mhd_init", []),
+    ("mhd_pipeline.cu", "mhd_pipeline", []),
+    ("mhd_selftest.cu", "mhd_selftest", []),
 ]
 
 

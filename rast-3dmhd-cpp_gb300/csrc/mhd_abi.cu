@@ -165,23 +165,9 @@ int fused_step(mhd_ctx* ctx, double dt, const double* dtp = nullptr) {
     }
     rc = sync_zghosts(ctx);
     if (rc) return rc;
-    const double gam[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
-    const double zet[3] = {ctx->k.ZETA1, ctx->k.ZETA2, 0.0};
     for (int s = 0; s < 3; s++) {
-        FusedArgs a{};
-        a.g = ctx->g;
-        a.c = ctx->c;
-        a.k = ctx->coef;
-        a.U = fields_of(ctx, ctx->U[ctx->cur]);
-        a.Uo = fields_of(ctx, ctx->U[1 - ctx->cur]);
-        a.Z = fields_of(ctx, ctx->Zb);
-        a.FT = ctx->Fb ? ctx->Fb + (size_t)F_FT * ctx->ncell : nullptr;
-        a.gdt = gam[s] * dt;
-        a.zdt = zet[s] * dt;
+        FusedArgs a = ctxops::fused_args(ctx, s, dt, ctx->cur);
         a.dtp = dtp;
-        a.gam = gam[s];
-        a.zet = zet[s];
-        a.substage = s;
         cudaEvent_t* ev = nullptr;
         if (ctx->profiling) {
             if (ctx->prof_used + 2 > ctx->prof_events.size()) {
@@ -257,7 +243,12 @@ int set_profile(mhd_ctx* ctx, int field, const double* host) {
             d2[z] = (p - m) * cz2a[z] + (p + m - 2.0 * bg[z]) * cz2b[z];
         }
     }
+    for (int z = 0; z < nz; z++) {
+        ctx->h_zf[3 * (size_t)nz + z] = (float)ctx->h_bg[2 * (size_t)nz + z];
+        ctx->h_zf[4 * (size_t)nz + z] = (float)ctx->h_bg[3 * (size_t)nz + z];
+    }
     CK(cudaMemcpy(ctx->d_bg, ctx->h_bg.data(), sizeof(double) * 4 * nz, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz, cudaMemcpyHostToDevice));
     return MHD_OK;
 }
 
@@ -331,6 +322,7 @@ int fused32_step(mhd_ctx* ctx, double dt) {
         a.bgT = ctx->d_bg + nz;
         a.dzT0 = ctx->d_bg + 2 * nz;
         a.d2zT0 = ctx->d_bg + 3 * nz;
+        a.zf = reinterpret_cast<const float*>(ctx->d_bg + 4 * nz);
         a.gdt = gam[s] * dt;
         a.zdt = zet[s] * dt;
         a.substage = s;
@@ -360,6 +352,24 @@ int fused32_step(mhd_ctx* ctx, double dt) {
 }  // namespace
 
 namespace mhd::ctxops {
+FusedArgs fused_args(const mhd_ctx* ctx, int s, double dt, int in) {
+    const double gam[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
+    const double zet[3] = {ctx->k.ZETA1, ctx->k.ZETA2, 0.0};
+    FusedArgs a{};
+    a.g = ctx->g;
+    a.c = ctx->c;
+    a.k = ctx->coef;
+    a.U = ::fields_of(ctx, ctx->U[in]);
+    a.Uo = ::fields_of(ctx, ctx->U[1 - in]);
+    a.Z = ::fields_of(ctx, ctx->Zb);
+    a.FT = ctx->Fb ? ctx->Fb + (size_t)F_FT * ctx->ncell : nullptr;
+    a.gdt = gam[s] * dt;
+    a.zdt = zet[s] * dt;
+    a.gam = gam[s];
+    a.zet = zet[s];
+    a.substage = s;
+    return a;
+}
 void advance_time(mhd_ctx* c, double dt) {
     c->nit += 1;
     c->timc += dt;
@@ -509,8 +519,17 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     int arc = MHD_OK;
     if (ctx->fp32) {
         arc = alloc_f32(ctx, &ctx->U32[0]);
-        if (!arc && cudaMalloc(&ctx->d_bg, sizeof(double) * 4 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
-        if (!arc && cudaMemset(ctx->d_bg, 0, sizeof(double) * 4 * nz) != cudaSuccess) arc = MHD_ERR_CUDA;
+        // 4 x nz double profiles, then the [7][nz] float coefficient table (8 x nz doubles in all)
+        if (!arc && cudaMalloc(&ctx->d_bg, sizeof(double) * 8 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
+        if (!arc && cudaMemset(ctx->d_bg, 0, sizeof(double) * 8 * nz) != cudaSuccess) arc = MHD_ERR_CUDA;
+        ctx->h_zf.assign(7 * (size_t)nz, 0.0f);
+        for (int z = 0; z < nz; z++) {
+            for (int r = 0; r < 3; r++) ctx->h_zf[(size_t)r * nz + z] = (float)ctx->h_cz[(size_t)r * nz + z];
+            ctx->h_zf[5 * (size_t)nz + z] = (float)p.RKAPA[z];
+            ctx->h_zf[6 * (size_t)nz + z] = (float)p.DKAPA[z];
+        }
+        if (!arc && cudaMemcpy(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz,
+                               cudaMemcpyHostToDevice) != cudaSuccess) arc = MHD_ERR_CUDA;
     } else {
         arc = alloc_block(ctx, &ctx->U[0], 8);
     }
@@ -552,6 +571,9 @@ int mhd_destroy(mhd_ctx* ctx) {
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->slab_events) cudaEventDestroy(e);
+    if (ctx->s_up) cudaStreamDestroy(ctx->s_up);
+    if (ctx->s_down) cudaStreamDestroy(ctx->s_down);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MHD_OK;

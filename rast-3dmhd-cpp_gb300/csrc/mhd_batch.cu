@@ -128,6 +128,7 @@ void fill_args32(const mhd_batch* b, const std::vector<int>& cur0, std::vector<F
                 a.bgT = c->d_bg + nz;
                 a.dzT0 = c->d_bg + 2 * nz;
                 a.d2zT0 = c->d_bg + 3 * nz;
+                a.zf = reinterpret_cast<const float*>(c->d_bg + 4 * nz);
                 a.gdt = gam[s] * b->dt[i];
                 a.zdt = zet[s] * b->dt[i];
                 a.timt = c->timt;

@@ -106,6 +106,8 @@ struct FusedArgs {
     // when dtp is set, gdt = gam * dtp[0] and zdt = zet * dtp[0]
     const double* dtp;
     double gam, zet;
+    // interior z planes [zlo, zhi) of a single-instance launch (zhi = 0: all)
+    int zlo, zhi;
 };
 // Device time-step record of mhd_steps_cfl: [0] DT in use (0 once halted),
 // [1] TIMT, [2] UMACH, [3] halt flag (DT < 1e-8), [4] the CFL DT computed
@@ -128,6 +130,8 @@ int fused_batch_occupancy_uxy(unsigned sw, int tile, int* blocks_per_sm);
 int fused_batch_occupancy_gen(unsigned sw, int tile, int* blocks_per_sm);
 int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, int nblocks, cudaStream_t st);
 int fused_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
+// BCON of one wall (0 = bottom plane 1, 1 = top plane nz-2) or both (wall = -1)
+int fused_bcon_wall(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, int wall, cudaStream_t st);
 
 // FP32-storage path (fields stored in FP32, RO and TT as deviations from FP64
 // reference profiles rho0(z), T0(z)).
@@ -144,6 +148,7 @@ struct Fused32Args {
     double* FT;    // FP64 persistent temperature right-hand side (lShr only)
     const double *bgR, *bgT;     // reference profiles rho0(z), T0(z)
     const double *dzT0, *d2zT0;  // their premultiplied first and second z derivatives
+    const float* zf;             // [7][nz] float cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA
     double gdt, zdt;
     double timt;
     int substage;

@@ -45,10 +45,16 @@ struct mhd_ctx {
     double* d_bg = nullptr;     // rho0, T0, dzT0, d2zT0 (4 x nz)
     std::vector<double> h_bg;   // host copy of the four profiles
     std::vector<double> h_cz;   // cz1, cz2a, cz2b (3 x nz)
+    // float copies of the per-z coefficients of the FP32 kernels, [7][nz]:
+    // cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA (device copy after d_bg's 4 x nz doubles)
+    std::vector<float> h_zf;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     bool profiling = false;
     std::vector<cudaEvent_t> prof_events;  // pairs around each substage launch
     size_t prof_used = 0;
+    // host-to-host steps: copy streams and per-slab events (created on first use)
+    cudaStream_t s_up = nullptr, s_down = nullptr;
+    std::vector<cudaEvent_t> slab_events;
 };
 
 namespace mhd::ctxops {
@@ -62,4 +68,7 @@ Fields8 fields_of(const mhd_ctx* c, double* base);
 int fail(mhd_ctx* c, int code, const std::string& msg);
 // one completed step of length dt: nIt, TIMC and TIMT advance as 3dmhdsub.h:150-152
 void advance_time(mhd_ctx* c, double dt);
+// FusedArgs of substage s (0..2) of the fused FP64 step reading state buffer
+// U[in] and writing U[1-in]
+FusedArgs fused_args(const mhd_ctx* c, int s, double dt, int in);
 }  // namespace mhd::ctxops

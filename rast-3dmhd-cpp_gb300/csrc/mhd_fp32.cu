@@ -18,6 +18,7 @@
 // The z-march, the shared-memory ring and the ghost-image stores follow the
 // FP64 kernel in mhd_fused.cu.
 #include "mhd_common.cuh"
+#include "mhd_convert.cuh"
 
 namespace mhd {
 namespace {
@@ -66,8 +67,8 @@ __device__ __forceinline__ void load_plane32(const Fused32Args& a, unsigned char
         const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
         const float ru = a.U.p[S_RU][i], rv = a.U.p[S_RV][i], rw = a.U.p[S_RW][i];
         const float dt = a.U.p[S_TT][i], dro = a.U.p[S_RO][i];
-        const double ro = r0 + (double)dro, tt = t0 + (double)dt;
-        const float ri = 1.0f / (float)ro;
+        const double ro = r0 + widen_f32(dro), tt = t0 + widen_f32(dt);
+        const float ri = 1.0f / narrow_f64(ro);
         r.p[k] = ro * tt;
         r.f[F_RU * kPlane + k] = ru;
         r.f[F_RV * kPlane + k] = rv;
@@ -122,6 +123,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
     const float ohm = (float)(c.OBETA * c.ORM * c.OCV);
     const float tmpc = (float)(c.OCV / c.REPR);
     const float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
+    const float omz = (float)c.OMZ, omx = (float)c.OMX;
 
     load_plane32<SW>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
     load_plane32<SW>(a, ring, zb % 3, zb, x0, y0);
@@ -145,7 +147,8 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             auto ZP = [&](int q) { return Pp[q * kPlane + pc]; };
             auto ZM = [&](int q) { return Pm[q * kPlane + pc]; };
             const double cz1d = a.k.cz1[z];
-            const float cz1 = (float)cz1d, cz2a = (float)a.k.cz2a[z], cz2b = (float)a.k.cz2b[z];
+            const int nzz = g.nz;
+            const float cz1 = a.zf[z], cz2a = a.zf[nzz + z], cz2b = a.zf[2 * nzz + z];
             auto Dx = [&](int q) { return (XP(q) - XM(q)) * cx1; };
             auto Dy = [&](int q) { return (YP(q) - YM(q)) * cy1; };
             auto Dz = [&](int q) { return (ZP(q) - ZM(q)) * cz1; };
@@ -163,9 +166,9 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             };
 
             const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
-            const double ro = a.bgR[z] + (double)C0(F_DRO);
-            const double tt = a.bgT[z] + (double)C0(F_DT);
-            const float ri = C0(F_RI), ttf = (float)tt;
+            const double ro = a.bgR[z] + widen_f32(C0(F_DRO));
+            const double tt = a.bgT[z] + widen_f32(C0(F_DT));
+            const float ri = C0(F_RI), ttf = narrow_f64(tt);
             const float u = C0(F_U), v = C0(F_V), w = C0(F_W);
 
             // ---- FP64: pressure gradient and gravity (3dmhdsub.h:266-272)
@@ -193,12 +196,12 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             fw -= fmaf(ZP(F_RW), ZP(F_W), -ZM(F_RW) * ZM(F_W)) * cz1;
 
             // ---- temperature (deviation stencils plus the FP64 profile's derivatives)
-            const float Tz = (float)a.dzT0[z] + Dz(F_DT);
+            const float Tz = a.zf[3 * nzz + z] + Dz(F_DT);
             float ft = 0.f;
             if constexpr (!SW::lShr) ft = -fmaf(u, Dx(F_DT), fmaf(v, Dy(F_DT), w * Tz));
             {
-                const float lapT = D2x(F_DT) + D2y(F_DT) + ((float)a.d2zT0[z] + D2z(F_DT));
-                ft = fmaf(ri * tmpc, fmaf((float)c.RKAPA[z], lapT, (float)c.DKAPA[z] * Tz), ft);
+                const float lapT = D2x(F_DT) + D2y(F_DT) + (a.zf[4 * nzz + z] + D2z(F_DT));
+                ft = fmaf(ri * tmpc, fmaf(a.zf[5 * nzz + z], lapT, a.zf[6 * nzz + z] * Tz), ft);
             }
 
             // ---- viscous Laplacians and cross terms
@@ -237,10 +240,10 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 ft = fmaf(-ocv * ttf, ux + vy + wz, ft);
             }
             if constexpr (SW::lRot) {
-                fu = fmaf((float)c.OMZ, C0(F_RV), fu);
-                fv = fmaf(-(float)c.OMZ, C0(F_RU), fv);
-                fv = fmaf((float)c.OMX, C0(F_RW), fv);
-                fw = fmaf(-(float)c.OMX, C0(F_RV), fw);
+                fu = fmaf(omz, C0(F_RV), fu);
+                fv = fmaf(-omz, C0(F_RU), fv);
+                fv = fmaf(omx, C0(F_RW), fv);
+                fw = fmaf(-omx, C0(F_RV), fw);
             }
             float w1 = 0, w2 = 0, w3 = 0;
             if constexpr (SW::lMag) {
@@ -290,10 +293,10 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             }
 
             // ---- FP64 RK3 register (3dmhdsub.h:168-192)
-            double ftd = (double)ft;
+            double ftd = widen_f32(ft);
             if constexpr (SW::lShr) ftd += a.FT[i];
-            const double fl[8] = {fu64 + (double)fu, fv64 + (double)fv, fw64 + (double)fw, ftd, (double)fr,
-                                  (double)w1, (double)w2, (double)w3};
+            const double fl[8] = {fu64 + widen_f32(fu), fv64 + widen_f32(fv), fw64 + widen_f32(fw), ftd,
+                                  widen_f32(fr), widen_f32(w1), widen_f32(w2), widen_f32(w3)};
             const int nf = SW::lMag ? 8 : 5;
             const double r0z = a.bgR[z], t0z = a.bgT[z];
 #pragma unroll
@@ -305,7 +308,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 const double zf = a.Z.p[f][i];
                 const double un = fma(a.gdt, fl[f], zf);
                 const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
-                store32_with_images(a.Uo.p[f], g, z, y, x, (float)(un - prof));
+                store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
                 a.Z.p[f][i] = (a.substage < 2) ? fma(a.zdt, fl[f], un) : un;
             }
             if constexpr (SW::lShr) a.FT[i] = ftd;
@@ -317,7 +320,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
 
 // one instance: grid (x tiles, y tiles, z chunks)
 template <class SW>
-__global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
+__global__ void __launch_bounds__(kThreads, 3) k_substage32(Fused32Args a) {
     extern __shared__ __align__(16) unsigned char ring[];
     const int nPz = a.g.nz - 2;
     const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_substage32(Fused32Args a) {
 // ragged batch: persistent CTAs take (instance, tile x, tile y, z range) items
 // (w = first plane | end plane << 16) from a counter that is zero at launch
 template <class SW>
-__global__ void __launch_bounds__(kThreads) k_substage32_batch(const Fused32Args* __restrict__ args,
+__global__ void __launch_bounds__(kThreads, 3) k_substage32_batch(const Fused32Args* __restrict__ args,
                                                                const int4* __restrict__ items, int nitems,
                                                                int* counter) {
     extern __shared__ __align__(16) unsigned char ring[];

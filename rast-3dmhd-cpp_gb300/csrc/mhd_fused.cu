@@ -23,19 +23,20 @@ constexpr int kMinBlocks = DefaultTile::kThreads >= 256 ? 2 : 3;
 template <class SW, bool UXY>
 __global__ void __launch_bounds__(DefaultTile::kThreads, kMinBlocks) k_substage(FusedArgs a) {
     extern __shared__ double ring[];
-    const int nPz = a.g.nz - 2;
-    const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);
-    const int ze = 1 + (int)((long long)nPz * (blockIdx.z + 1) / gridDim.z);
+    const int lo = a.zhi > 0 ? a.zlo : 1;
+    const int nz = (a.zhi > 0 ? a.zhi : a.g.nz - 1) - lo;
+    const int zb = lo + (int)((long long)nz * blockIdx.z / gridDim.z);
+    const int ze = lo + (int)((long long)nz * (blockIdx.z + 1) / gridDim.z);
     substage_tile<SW, DefaultTile, UXY>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
 }
 
 template <class SW>
-__global__ void k_bcon_ghost(Grid g, Consts c, Fields8 U, double timt) {
+__global__ void k_bcon_ghost(Grid g, Consts c, Fields8 U, double timt, int wall0, int nwalls) {
     const int nPx = g.nx - 2, nPy = g.ny - 2;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * nPx * nPy) return;
+    if (t >= nwalls * nPx * nPy) return;
     const int r = t % (nPx * nPy);
-    bcon_cell<SW>(g, c, U, timt, t / (nPx * nPy), 1 + r % nPx, 1 + r / nPx);
+    bcon_cell<SW>(g, c, U, timt, wall0 + t / (nPx * nPy), 1 + r % nPx, 1 + r / nPx);
 }
 
 int choose_chunks(long long tiles, int slots, int nPz) {
@@ -68,7 +69,8 @@ int launch_t(const FusedArgs& a, cudaStream_t st) {
         slots = sms * (per_sm > 0 ? per_sm : 1);
     }
     const int nbx = (a.g.nx - 2 + T::kTX - 1) / T::kTX, nby = (a.g.ny - 2 + T::kTY - 1) / T::kTY;
-    const int chunks = choose_chunks((long long)nbx * nby, slots, a.g.nz - 2);
+    const int planes = a.zhi > 0 ? a.zhi - a.zlo : a.g.nz - 2;
+    const int chunks = choose_chunks((long long)nbx * nby, slots, planes);
     k_substage<SW, UXY><<<dim3(nbx, nby, chunks), T::kThreads, smem, st>>>(a);
     return (int)cudaGetLastError();
 }
@@ -79,9 +81,10 @@ void launch_substage(const FusedArgs& a, cudaStream_t st, int* rc) {
 }
 
 template <class SW>
-void launch_bcon_ghost(const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st) {
-    const int n = 2 * (g.nx - 2) * (g.ny - 2);
-    k_bcon_ghost<SW><<<(n + 127) / 128, 128, 0, st>>>(g, c, U, timt);
+void launch_bcon_ghost(const Grid& g, const Consts& c, Fields8 U, double timt, int wall, cudaStream_t st) {
+    const int nwalls = wall < 0 ? 2 : 1, wall0 = wall < 0 ? 0 : wall;
+    const int n = nwalls * (g.nx - 2) * (g.ny - 2);
+    k_bcon_ghost<SW><<<(n + 127) / 128, 128, 0, st>>>(g, c, U, timt, wall0, nwalls);
 }
 
 }  // namespace
@@ -93,7 +96,12 @@ int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st) {
 }
 
 int fused_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st) {
-    MHD_DISPATCH_SW(sw, launch_bcon_ghost, g, c, U, timt, st);
+    MHD_DISPATCH_SW(sw, launch_bcon_ghost, g, c, U, timt, -1, st);
+    return (int)cudaGetLastError();
+}
+
+int fused_bcon_wall(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, int wall, cudaStream_t st) {
+    MHD_DISPATCH_SW(sw, launch_bcon_ghost, g, c, U, timt, wall, st);
     return (int)cudaGetLastError();
 }
 

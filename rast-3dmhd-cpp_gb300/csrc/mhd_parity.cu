@@ -16,6 +16,7 @@
 // the scale factor is applied last; a scale of 1 is the identity and -1 a
 // negation.
 #include "mhd_common.cuh"
+#include "mhd_convert.cuh"
 
 namespace mhd {
 namespace {
@@ -547,6 +548,82 @@ __device__ __forceinline__ bool nonzero_bits(double d) {
     return (((unsigned)__double2hiint(d) & 0x7fffffffu) | (unsigned)__double2loint(d)) != 0u;
 }
 
+// FP32 estimates of cell i's fast-mode candidate a0 and of mc (both certified
+// to 1.2e-6 when `ok`), and whether its momenta are not all exactly zero.
+template <bool MAG>
+__device__ __forceinline__ void cfl_estimate(const Fields8& U, long long i, float ddf, float gam_f, float obeta_f,
+                                             double rod, float& a0, float& mc, bool& ok, bool& nz) {
+    const double rud = U.p[S_RU][i], rvd = U.p[S_RV][i], rwd = U.p[S_RW][i], ttd = U.p[S_TT][i];
+    nz = nonzero_bits(rud) || nonzero_bits(rvd) || nonzero_bits(rwd);
+    const float ru = trunc_to_f32(rud), rv = trunc_to_f32(rvd), rw = trunc_to_f32(rwd);
+    const float ro = trunc_to_f32(rod), tt = trunc_to_f32(ttd);
+    const float ir = __frcp_rn(ro);
+    const float sq = __fadd_rn(__fadd_rn(__fmul_rn(ru, ru), __fmul_rn(rv, rv)), __fmul_rn(rw, rw));
+    const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
+    float G = __fmul_rn(gam_f, tt);
+    if constexpr (MAG) {
+        const float bx = trunc_to_f32(U.p[S_BX][i]), by = trunc_to_f32(U.p[S_BY][i]), bz = trunc_to_f32(U.p[S_BZ][i]);
+        const float b2 = __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
+        G = __fadd_rn(G, __fmul_rn(__fmul_rn(obeta_f, b2), ir));
+    }
+    const float uuf = __fadd_rn(__fadd_rn(uuk, G), __fmul_rn(2.0f, __fsqrt_rn(__fmul_rn(uuk, G))));
+    mc = __fdiv_rn(uuk, tt);
+    a0 = __fmul_rn(ddf, rsqrtf(uuf));
+    ok = (ro >= 0x1p-20f && ro <= 0x1p20f) && (tt >= 0x1p-20f && tt <= 0x1p20f) && isfinite(uuf) &&
+         isfinite(mc) && isfinite(a0);
+}
+
+// Whether a row takes the filtered path (see k_cfl_rows), with its DD.
+__device__ __forceinline__ bool cfl_fast_row(const Grid& g, const Consts& c, int y, int z, double& DDyz) {
+    DDyz = cfl_dd_yz(c, y, z);
+    const double P1 = 0.5f * DDyz * DDyz * c.REPR * c.CV;  // prefix of cfl_a1
+    const double P2 = 0.375f * DDyz * DDyz * c.RE;         // prefix of cfl_a2
+    const bool consts_ok = (c.GAMMA >= 0x1p-10 && c.GAMMA <= 0x1p10) && (c.OBETA >= 0.0 && c.OBETA <= 0x1p30);
+    return consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 && c.RKAPA[z] > 0.0;
+}
+
+// Seeds of the filter: the smallest a0 estimate and the largest mc estimate
+// (momenta not all zero) over every kCflSeedStride-th row, as ordered integer
+// keys (0 = nothing seen).  Any estimate that some certified cell attains is a
+// valid filter base, so the row kernel may start from these.
+constexpr int kCflSeedStride = 8;
+template <bool MAG>
+__global__ void k_cfl_seed(Grid g, Consts c, Fields8 U, unsigned* seed) {
+    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
+    const long long nrows = ((long long)nPy * nPz + kCflSeedStride - 1) / kCflSeedStride;
+    const int lane = threadIdx.x & 31;
+    const float gam_f = (float)c.GAMMA, obeta_f = (float)c.OBETA;
+    float best_a = INFINITY, best_m = 0.0f;
+    for (long long q = (long long)(blockIdx.x * blockDim.x + threadIdx.x) / 32; q < nrows;
+         q += (long long)gridDim.x * blockDim.x / 32) {
+        const long long r = q * kCflSeedStride;
+        const int y = 1 + (int)(r % nPy), z = 1 + (int)(r / nPy);
+        double DDyz;
+        if (!cfl_fast_row(g, c, y, z, DDyz)) continue;
+        const float ddf = narrow_f64(DDyz);
+        const long long row = (long long)z * g.sz + (long long)y * g.sy;
+        for (int x = 1 + lane; x <= nPx; x += 32) {
+            float a0, mc;
+            bool ok, nz;
+            cfl_estimate<MAG>(U, row + x, ddf, gam_f, obeta_f, U.p[S_RO][row + x], a0, mc, ok, nz);
+            if (ok) {
+                best_a = fminf(best_a, a0);
+                if (nz) best_m = fmaxf(best_m, mc);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        best_a = fminf(best_a, __shfl_xor_sync(0xffffffffu, best_a, o));
+        best_m = fmaxf(best_m, __shfl_xor_sync(0xffffffffu, best_m, o));
+    }
+    if (lane == 0) {
+        // positive floats order like their bit patterns
+        if (best_a < INFINITY) atomicMax(&seed[0], 0x7f800000u - __float_as_uint(best_a));
+        if (best_m > 0.0f) atomicMax(&seed[1], __float_as_uint(best_m));
+    }
+}
+
 constexpr int kCflK = 8;                         // cells per lane in one pass over a row
 constexpr int kCflWarps = 8;                     // 256 threads
 constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x the approximation error
@@ -559,91 +636,83 @@ constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x t
 //   * a1, a2 are products/quotients of ro with positive row constants and a3
 //     depends on DD alone; rounding is monotone, so their row minima are the
 //     candidates of the row's smallest ro (an exact FP64 min);
-//   * a0 = DD/sqrt(UU') is smallest where UU' is largest; UU' and mc are
-//     estimated in FP32 from inputs truncated to 23 bits (error below 1.2e-6
-//     for inputs in the accepted ranges), the cells whose estimate lies within
-//     2^-16 of the pass's largest are evaluated exactly, and every cell whose
-//     estimate is not certified (out-of-range input, non-finite value) too.
-// The row's exact maximum of mc and minimum of a0 are therefore among the cells
+//   * mc and a0 = DD/sqrt(UU') are estimated in FP32 from inputs truncated to
+//     23 bits (error below 1.2e-6 for inputs in the accepted ranges); a cell is
+//     evaluated exactly when its estimate lies within 2^-16 of the best
+//     estimate the warp has seen so far (the running maximum of mc, minimum of
+//     a0, the current pass included), or when its estimate is not certified
+//     (out-of-range input, non-finite value).  The best estimate seen so far
+//     is never better than the best over all of the warp's cells, and the cell
+//     holding the warp's exact extremum has an estimate within the error
+//     bound of that, so it is always evaluated exactly.
+// The exact maximum of mc and minimum of a0 are therefore among the cells
 // evaluated exactly, and the result equals the cell-by-cell reduction bit for
-// bit.  Rows with varying DD, and launches whose constants break the
+// bit; after the first passes only new near-extremes are evaluated.  Rows with varying DD, and launches whose constants break the
 // monotonicity (non-positive factors), evaluate every cell exactly.
 template <bool MAG>
-__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, Fields8 U, double* part) {
+__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, Fields8 U, const unsigned* seed,
+                                                             double* part) {
     __shared__ int list[kCflWarps][32 * kCflK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
     const long long nrows = (long long)nPy * nPz;
     const double OGAMMA = 1.0f / c.GAMMA;
-    const bool consts_ok = (c.GAMMA >= 0x1p-10 && c.GAMMA <= 0x1p10) && (c.OBETA >= 0.0 && c.OBETA <= 0x1p30);
     const float gam_f = (float)c.GAMMA, obeta_f = (float)c.OBETA;
     double um = 0.0f, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
+    // the best estimates so far (warp-uniform), starting from the seeds
+    float run_a = seed[0] ? __uint_as_float(0x7f800000u - seed[0]) : INFINITY;
+    float run_m = seed[1] ? __uint_as_float(seed[1]) : -INFINITY;
     for (long long r = (long long)blockIdx.x * kCflWarps + wid; r < nrows; r += (long long)gridDim.x * kCflWarps) {
         const int y = 1 + (int)(r % nPy), z = 1 + (int)(r / nPy);
         const long long row = (long long)z * g.sz + (long long)y * g.sy;
-        const double DDyz = cfl_dd_yz(c, y, z);
-        const double P1 = 0.5f * DDyz * DDyz * c.REPR * c.CV;  // prefix of cfl_a1
-        const double P2 = 0.375f * DDyz * DDyz * c.RE;         // prefix of cfl_a2
-        const bool fast = consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 &&
-                          c.RKAPA[z] > 0.0;
+        double DDyz;
+        const bool fast = cfl_fast_row(g, c, y, z, DDyz);
         if (!fast) {
             for (int x = 1 + lane; x <= nPx; x += 32) cfl_cell<MAG>(g, c, U, x, y, z, OGAMMA, um, w0, w1, w2, w3);
             continue;
         }
         double mro = __longlong_as_double(0x7ff0000000000000LL);  // +inf: no cell yet
+        const float ddf = narrow_f64(DDyz);
         for (int x0 = 1; x0 <= nPx; x0 += 32 * kCflK) {
-            float uA[kCflK], mA[kCflK];
+            float aA[kCflK], mA[kCflK];
             unsigned okm = 0u, nzm = 0u, valid = 0u;
-            float Mu = -INFINITY, Mm = -INFINITY;
+            float Ma = INFINITY, Mm = -INFINITY;
 #pragma unroll
             for (int k = 0; k < kCflK; k++) {
                 const int x = x0 + k * 32 + lane;
-                uA[k] = 0.0f;
+                aA[k] = 0.0f;
                 mA[k] = 0.0f;
                 if (x > nPx) continue;
                 valid |= 1u << k;
                 const long long i = row + x;
-                const double rud = U.p[S_RU][i], rvd = U.p[S_RV][i], rwd = U.p[S_RW][i];
-                const double rod = U.p[S_RO][i], ttd = U.p[S_TT][i];
+                const double rod = U.p[S_RO][i];
                 mro = (rod < mro) ? rod : mro;
-                const bool nz = nonzero_bits(rud) || nonzero_bits(rvd) || nonzero_bits(rwd);
-                const float ru = trunc_to_f32(rud), rv = trunc_to_f32(rvd), rw = trunc_to_f32(rwd);
-                const float ro = trunc_to_f32(rod), tt = trunc_to_f32(ttd);
-                const float ir = __frcp_rn(ro);
-                const float sq = __fadd_rn(__fadd_rn(__fmul_rn(ru, ru), __fmul_rn(rv, rv)), __fmul_rn(rw, rw));
-                const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
-                float G = __fmul_rn(gam_f, tt);
-                if constexpr (MAG) {
-                    const float bx = trunc_to_f32(U.p[S_BX][i]), by = trunc_to_f32(U.p[S_BY][i]),
-                                bz = trunc_to_f32(U.p[S_BZ][i]);
-                    const float b2 = __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
-                    G = __fadd_rn(G, __fmul_rn(__fmul_rn(obeta_f, b2), ir));
-                }
-                const float uuf = __fadd_rn(__fadd_rn(uuk, G), __fmul_rn(2.0f, __fsqrt_rn(__fmul_rn(uuk, G))));
-                const float mc = __fdiv_rn(uuk, tt);
-                const bool ok = (ro >= 0x1p-20f && ro <= 0x1p20f) && (tt >= 0x1p-20f && tt <= 0x1p20f) &&
-                                isfinite(uuf) && isfinite(mc);
-                uA[k] = uuf;
+                float a0, mc;
+                bool ok, nz;
+                cfl_estimate<MAG>(U, i, ddf, gam_f, obeta_f, rod, a0, mc, ok, nz);
+                aA[k] = a0;
                 mA[k] = mc;
                 if (ok) {
                     okm |= 1u << k;
-                    Mu = fmaxf(Mu, uuf);
+                    Ma = fminf(Ma, a0);
                     if (nz) Mm = fmaxf(Mm, mc);
                 }
                 if (nz) nzm |= 1u << k;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                Mu = fmaxf(Mu, __shfl_xor_sync(0xffffffffu, Mu, o));
+                Ma = fminf(Ma, __shfl_xor_sync(0xffffffffu, Ma, o));
                 Mm = fmaxf(Mm, __shfl_xor_sync(0xffffffffu, Mm, o));
             }
-            const float tu = Mu - kCflTau * Mu;
-            const float tm = (Mm >= 0x1p-40f) ? Mm - kCflTau * Mm : -INFINITY;
+            run_a = fminf(run_a, Ma);
+            run_m = fmaxf(run_m, Mm);
+            const float ta = run_a + kCflTau * run_a;
+            const float tm = (run_m >= 0x1p-40f) ? run_m - kCflTau * run_m : -INFINITY;
             int n = 0;
 #pragma unroll
             for (int k = 0; k < kCflK; k++) {
                 const bool v = (valid >> k) & 1u, ok = (okm >> k) & 1u, nz = (nzm >> k) & 1u;
-                const bool cand = v && (!ok || uA[k] >= tu || (nz && mA[k] >= tm));
+                const bool cand = v && (!ok || aA[k] <= ta || (nz && mA[k] >= tm));
                 const unsigned bal = __ballot_sync(0xffffffffu, cand);
                 if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
                 n += __popc(bal);
@@ -677,15 +746,40 @@ __global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, F
     write_cfl_partials(um, w0, w1, w2, w3, part);
 }
 
-// Launch the row reduction; returns the number of partial blocks.
+// Launch the row reduction with one wave of resident blocks (each warp then
+// sees many rows, so its running estimates filter most cells); returns the
+// number of partial blocks.
 int launch_cfl_rows(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
                     cudaStream_t st) {
+    static int wave[2] = {0, 0};
+    int& w = wave[mag ? 1 : 0];
+    if (!w) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (mag) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<true>, kCflWarps * 32, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<false>, kCflWarps * 32, 0);
+        w = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }
     const long long nrows = (long long)(g.ny - 2) * (g.nz - 2);
     long long nb = (nrows + kCflWarps - 1) / kCflWarps;
     if (nb < 1) nb = 1;
+    if (nb > w) nb = w;
     if (nb > max_blocks) nb = max_blocks;
-    if (mag) k_cfl_rows<true><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, partials);
-    else k_cfl_rows<false><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, partials);
+    // two seed words after the largest partial block (5 x max_blocks doubles)
+    unsigned* seed = reinterpret_cast<unsigned*>(partials + 5 * (size_t)max_blocks);
+    cudaMemsetAsync(seed, 0, 2 * sizeof(unsigned), st);
+    const long long srows = (nrows + kCflSeedStride - 1) / kCflSeedStride;
+    long long sb = (srows * 32 + 255) / 256;
+    if (sb > w) sb = w;
+    if (sb < 1) sb = 1;
+    if (mag) {
+        k_cfl_seed<true><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
+        k_cfl_rows<true><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
+    } else {
+        k_cfl_seed<false><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
+        k_cfl_rows<false><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
+    }
     return (int)nb;
 }
 

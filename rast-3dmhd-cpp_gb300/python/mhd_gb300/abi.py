@@ -102,6 +102,8 @@ SIGNATURES = {
     "mhd_step": [C.c_void_p, C.c_double, C.POINTER(MhdDiag)],
     "mhd_steps": [C.c_void_p, C.c_int, C.c_double],
     "mhd_steps_cfl": [C.c_void_p, C.c_int, C.POINTER(MhdDiag)],
+    "mhd_step_host": [C.c_void_p, _DP, _DP, C.c_double],
+    "mhd_selftest_convert": [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],
     "mhd_batch_create": [C.POINTER(C.c_void_p), _DP, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)],

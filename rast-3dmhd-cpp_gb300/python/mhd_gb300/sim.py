@@ -151,6 +151,21 @@ class Simulation:
     def steps(self, n: int, dt: float | None = None) -> None:
         self._ck(self.L.mhd_steps(self.ctx, n, self.case.dt if dt is None else dt))
 
+    def step_host(self, host_in, host_out, dt: float | None = None) -> None:
+        """One fused step from a host state to a host state (mhd_step_host);
+        host_in / host_out are float64 arrays of nf x nz x ny x nx (or None),
+        the upload / step / download overlapped slab by slab."""
+        def ptr(a):
+            if a is None:
+                return None
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.case.nfields * self.ncell_all
+            return _dp(a)
+        self._ck(self.L.mhd_step_host(self.ctx, ptr(host_in), ptr(host_out), self.case.dt if dt is None else dt))
+
+    @property
+    def ncell_all(self) -> int:
+        return self.case.nx * self.case.ny * self.case.nz
+
     def steps_cfl(self, n: int, check: bool = True) -> tuple[int, dict]:
         """n steps with the CFL dt of each (the reference's run mode).
         Returns (status, diag); status MHD_ERR_DT_TOO_SMALL is the halt of

@@ -1,11 +1,14 @@
 """FP32-storage form: fields stored and stenciled in FP32 (RO and TT as
 deviations from FP64 reference profiles), pressure/gravity, the RK3
 register and the reductions in FP64.  Checked against the FP64 paths."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
 from gpu_util import oracle_for, rel_err
 from mhd_gb300.case import STATE_FIELDS, config0, initial_state, small_cases
+from mhd_gb300 import abi
 from mhd_gb300.sim import Simulation
 
 pytestmark = pytest.mark.gpu
@@ -102,3 +105,14 @@ def test_unfused_calls_rejected_for_fp32():
     with pytest.raises(MhdError):
         sim.fluxes()
     sim.close()
+
+
+def test_integer_pipe_conversions_match_hardware():
+    """The FP32-storage kernels widen and narrow with integer operations
+    (mhd_convert.cuh) to keep conversions off the FP64 pipe; on 2^24 test
+    patterns (random bits, rounding ties, the float range edges, subnormals)
+    they equal cvt.f64.f32 and cvt.rn.f32.f64 bit for bit."""
+    L = abi.load()
+    n = C.c_longlong(-1)
+    abi.check(L.mhd_selftest_convert(1 << 24, 20261203, C.byref(n)))
+    assert n.value == 0
