@@ -201,6 +201,23 @@ typedef struct mhd_fluxes_noalloc_args {
 } mhd_fluxes_noalloc_args;
 int mhd_fluxes_noalloc(const mhd_fluxes_noalloc_args* args, void* stream);
 
+/* ---- plume terms ---------------------------------------------------------- */
+/* Parameters of the plume terms (3dmhd.cpp:413-426, par[12..15,52,54]): the
+ * cooling spot on the top wall (TP != 0 with iTCon 0 or 1,
+ * 3dmhdsub.h:750-778) and the internal heat sink of iTCon 2
+ * (3dmhdsub.h:443-459), centred at (XP, YP, ZP) with width HH, switched on
+ * over TC (and QFH for the sink).  EXX, WYY, ZEE are the coordinates of every
+ * x, y, z index (nx, ny, nz entries, ghosts included; host memory, read
+ * during the call).  A context whose switches need these terms rejects
+ * steps with MHD_ERR_INVALID until this call; the Gaussian factors are
+ * computed here, on the host, with the reference's expressions, so the
+ * unfused path stays bit-exact with it. */
+typedef struct mhd_plume {
+    double XP, YP, ZP, HH, TC, QFH;
+    const double *EXX, *WYY, *ZEE;
+} mhd_plume;
+int mhd_set_plume(mhd_ctx* ctx, const mhd_plume* plume);
+
 /* ---- fused time stepping ------------------------------------------------ */
 /* One RK3 step, replacing step() (3dmhdsub.h:31-153).  dt > 0: fixed step;
  * dt <= 0: the reference's CFL step (then the call blocks for the dt).

@@ -28,6 +28,9 @@
 #define ORC_PRAGMA(x)
 #endif
 
+/* square() of 3dmhdutils.h */
+static inline double sq(double v) { return v * v; }
+
 #define SWEEP(...) SWEEP_(__VA_ARGS__)
 #define SWEEP_(Z0, Z1, Y0, Y1, X0, X1, ...)                                     \
     do {                                                                        \
@@ -172,6 +175,18 @@ int orc_fluxes(const orc_params* p, orc_fields* f) {
     SWEEP(R_, FT[i] += ((D2Y(TT) * RO[i]) * p->RKAPA[z]) * tmp);
     SWEEP(R_, FT[i] += ((D2Z(TT) * RO[i]) * p->RKAPA[z]) * tmp);
     SWEEP(R_, FT[i] += ((D1Z(TT) * RO[i]) * p->DKAPA[z]) * tmp);
+
+    /* internal plume heat sink (iTCon 2), 3dmhdsub.h:443-459; RO holds 1/rho.
+     * log(2.0f) is the float overload in the reference's C++ (3dmhdphsic.h
+     * includes <math.h> before this code). */
+    if (p->iTCon == 2) {
+        const double CLN = (double)(-4.0f * logf(2.0f)) / p->HH / p->HH;
+        const double s = (p->TC != 0.0)
+                             ? p->TP * p->OCV * 0.5f * (1.0f + tanh((double)logf(2.0f) / p->QFH * (p->TIMT - p->TC)))
+                             : p->TP * p->OCV;
+        SWEEP(R_, FT[i] -= s * RO[i] * exp(CLN * sq(p->EXX[x] - p->XP) / p->HH) *
+                           exp(CLN * sq(p->WYY[y] - p->YP) / p->HH) * exp(CLN * sq(p->ZEE[z] - p->ZP) / p->HH));
+    }
 
     /* viscous Laplacians, 3dmhdsub.h:462-472 */
     SWEEP(R_, FU[i] += D2X(UU) * (p->ORE * p->C43));
@@ -404,9 +419,8 @@ int orc_bcon(const orc_params* p, orc_fields* f, double timt) {
     double* BZ = f->a[ORC_BZ];
     const int zl = 1, zr = nz - 1;
     const double RRT = 1.0f, RRB = -1.0f, RPP = 0.0f;
-    if ((p->TP != 0.0) && (p->iTCon == 0 || p->iTCon == 1)) return -1;
     if (p->izCon != 0 && p->izCon != 1) return -1;
-    if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 4) return -1;
+    if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 2 && p->iTCon != 4) return -1;
 
     /* top wall */
     if (p->lShr) {
@@ -417,7 +431,22 @@ int orc_bcon(const orc_params* p, orc_fields* f, double timt) {
               RV[i] = RO[i] * (p->C43 * RV[i + sz] / RO[i + sz] - p->C13 * RV[i + 2 * sz] / RO[i + 2 * sz]));
     }
     SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, RW[i] = 0.0f);
-    if (p->iTCon == 0 || p->iTCon == 4) {
+    if ((p->TP != 0.0) && (p->iTCon == 0 || p->iTCon == 1)) {
+        /* cooling spot on the top wall, 3dmhdsub.h:750-778 */
+        const double TPR = (p->TC != 0.0) ? p->TP + (1.0f - p->TP) * exp(-timt / p->TC) : p->TP;
+        const double CLN = (double)(-4.0f * logf(2.0f)) / p->HH / p->HH;
+        if (p->iTCon == 0) {
+            SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1,
+                  TT[i] = 1.0f - (1.0f - TPR) * exp(CLN * sq(p->EXX[x] - p->XP)) / p->HH *
+                                     exp(CLN * sq(p->WYY[y] - p->YP)) / p->HH);
+        } else {
+            const double DZ = 1.0f / (double)(p->nPz - 1) / p->dzzdz[zl];
+            SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1,
+                  TT[i] = p->C43 * TT[i + sz] - p->C13 * TT[i + 2 * sz] -
+                          p->C23 * DZ * (p->THETA - (p->THETA - TPR) * exp(CLN * sq(p->EXX[x] - p->XP)) / p->HH *
+                                                        exp(CLN * sq(p->WYY[y] - p->YP)) / p->HH));
+        }
+    } else if (p->iTCon == 0 || p->iTCon == 2 || p->iTCon == 4) {
         const int is4 = p->iTCon == 4;
         SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, TT[i] = 1.0f; if (is4 && x < nx / 2) TT[i] = 1.0f - p->TP);
     } else { /* iTCon == 1 with TP == 0: fixed flux */
@@ -502,13 +531,16 @@ double orc_cfl_dt(const orc_params* p, orc_fields* f, double* umach) {
     return p->SFF * dmin(dmin(w0, w1), w2);
 }
 
-int orc_steps(const orc_params* p, orc_fields* f, int n, double dt, double* timt, double* dt_out) {
+int orc_steps(const orc_params* p0, orc_fields* f, int n, double dt, double* timt, double* dt_out) {
+    orc_params q = *p0;  /* fluxes() sees the step's TIMT */
+    const orc_params* p = &q;
     double t = timt ? *timt : 0.0;
     const double timi = t;
     double timc = 0.0;
     for (int s = 0; s < n; s++) {
         double DT = dt;
         if (dt <= 0.0) DT = orc_cfl_dt(p, f, NULL);
+        q.TIMT = t;
         orc_rk_zeta0(p, f);
         orc_fluxes(p, f);
         orc_rk_gam(p, f, p->GAM1 * DT);

@@ -35,6 +35,12 @@ typedef struct orc_params {
     const double *dyydy, *d2yydy2, *DDY;
     const double *dzzdz, *d2zzdz2, *DDZ;
     const double *RKAPA, *DKAPA;
+    /* plume terms (3dmhdsub.h:443-459,750-778): coordinates (x nx, y ny, z nz
+     * entries; may be NULL when no plume term is active), parameters
+     * (3dmhd.cpp:413-426) and the simulation time TIMT the source sees */
+    const double *EXX, *WYY, *ZEE;
+    double XP, YP, ZP, HH, TC, QFH;
+    double TIMT;
 } orc_params;
 
 /* Field slots.  0-7 state, 8-15 right-hand sides, 16-23 RK register,

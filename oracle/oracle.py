@@ -21,7 +21,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
-from mhd_gb300.case import Case, STATE_FIELDS, FLUX_FIELDS, ZFIELDS, metrics  # noqa: E402
+from mhd_gb300.case import Case, STATE_FIELDS, FLUX_FIELDS, ZFIELDS, coordinates, metrics  # noqa: E402
 
 BUILD_DIR = HERE / "_build"
 LIB = BUILD_DIR / "libmhd_oracle.so"
@@ -50,7 +50,9 @@ class OrcParams(C.Structure):
                                            "RY", "ANG", "OMX", "OMZ", "RM", "ORM", "BETA", "OBETA", "TB", "TP",
                                            "SFF")] + \
                [(n, C.POINTER(C.c_double)) for n in ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY",
-                                                      "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")]
+                                                      "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")] + \
+               [(n, C.POINTER(C.c_double)) for n in ("EXX", "WYY", "ZEE")] + \
+               [(n, C.c_double) for n in ("XP", "YP", "ZP", "HH", "TC", "QFH", "TIMT")]
 
 
 class OrcFields(C.Structure):
@@ -105,6 +107,11 @@ class OracleSim:
         names = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
         for n, a in zip(names, self._metric_arrays):
             setattr(p, n, _dptr(a))
+        self._coord_arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in coordinates(case)]
+        for n, a in zip(("EXX", "WYY", "ZEE"), self._coord_arrays):
+            setattr(p, n, _dptr(a))
+        for k in ("XP", "YP", "ZP", "HH", "TC", "QFH"):
+            setattr(p, k, float(getattr(case, k)))
         self.L.orc_set_constants(C.byref(p), case.nPx, case.nPy, case.nPz)
         self.p = p
         self.f = OrcFields()
@@ -124,6 +131,7 @@ class OracleSim:
 
     # reference entry points -------------------------------------------------
     def fluxes(self) -> None:
+        self.p.TIMT = self.timt
         self.L.orc_fluxes(C.byref(self.p), C.byref(self.f))
 
     def step_block_ZETA0(self) -> None:

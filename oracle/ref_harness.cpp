@@ -10,7 +10,7 @@
  *
  * Input file (written by oracle/refcase.py): a global single-domain state
  * of (nPz+2) x (nPy+2) x (nPx+2) doubles per field, x fastest, plus the 1-D
- * metric arrays.  Each rank takes its slab (3dmhd.cpp:95-96 rank layout),
+ * metric arrays and (format version 2) the coordinate arrays EXX, WYY, ZEE.  Each rank takes its slab (3dmhd.cpp:95-96 rank layout),
  * calls communicate() once like main() does (3dmhd.cpp:142), then runs:
  *   mode 0  fluxes() once                              (3dmhdsub.h:194)
  *   mode 1  N fixed-dt RK3 steps: the body of step()    (3dmhdsub.h:116-152)
@@ -136,7 +136,8 @@ int main(int argc, char** argv) {
     const int gnx = nPx + ix, gny = nPy + iy, gnz = nPz + iz;
     const size_t nglob = (size_t)gnz * gny * gnx;
     const size_t n_metric = 3 * (size_t)gnx + 3 * (size_t)gny + 5 * (size_t)gnz;
-    const size_t need = sizeof(InHeader) + sizeof(double) * (n_metric + 9 * nglob);
+    const size_t n_coord = h.version >= 2 ? (size_t)gnx + gny + gnz : 0;
+    const size_t need = sizeof(InHeader) + sizeof(double) * (n_metric + 9 * nglob + n_coord);
     if (raw.size() < need) die("input truncated");
     const double* p = reinterpret_cast<const double*>(raw.data() + sizeof(InHeader));
     const double *g_dxxdx = p, *g_d2xxdx2 = p + gnx, *g_DDX = p + 2 * gnx;
@@ -147,6 +148,7 @@ int main(int argc, char** argv) {
                  *g_DKAPA = p + 4 * gnz;
     p += 5 * gnz;
     const double* g_fields = p; /* RU RV RW TT RO BX BY BZ FT */
+    const double* g_coord = p + 9 * nglob; /* EXX WYY ZEE (version >= 2) */
 
     /* Output: 24 global arrays (state 8, F 8, Z 8) then 16 + nsteps trailer doubles. */
     const int nsteps = h.nsteps > 0 ? h.nsteps : 0;
@@ -185,6 +187,12 @@ int main(int argc, char** argv) {
     load_zarr(g_DDZ, DDZ);
     load_zarr(g_RKAPA, RKAPA);
     load_zarr(g_DKAPA, DKAPA);
+    if (h.version >= 2) {
+        /* coordinates of the requested grid replace set()'s (plume terms, 3dmhdsub.h:443-459,750-778) */
+        for (int x = 0; x < nx; x++) EXX[x] = g_coord[x];
+        load_yarr(g_coord + gnx, WYY);
+        load_zarr(g_coord + gnx + gny, ZEE);
+    }
 
     data* fields_in[9] = {&RU, &RV, &RW, &TT, &RO, &BX, &BY, &BZ, &FT};
     for (int f = 0; f < 9; f++) {

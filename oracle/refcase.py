@@ -18,6 +18,7 @@ The reference tree is only needed to BUILD; the binaries land in
 """
 from __future__ import annotations
 
+import fcntl
 import hashlib
 import os
 import struct
@@ -31,7 +32,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
-from mhd_gb300.case import Case, STATE_FIELDS, FLUX_FIELDS, ZFIELDS, metrics  # noqa: E402
+from mhd_gb300.case import Case, STATE_FIELDS, FLUX_FIELDS, ZFIELDS, coordinates, metrics  # noqa: E402
 
 REF_DIR = Path(os.environ.get("MHD_REFERENCE_DIR", "/root/reference"))
 OUT_DIR = HERE / "_ref"
@@ -108,8 +109,8 @@ const int nCol = 0, nRow = 0, nTubes = nCol * nRow;
 def set_header(case: Case) -> str:
     """3dmhdset.h for one case: setup() fills ipar/par like 3dmhdset.h:7-24."""
     par = {0: case.RE, 1: case.PR, 2: case.THETA, 3: case.GRAV, 4: case.RY, 5: case.ANG,
-           6: case.RM, 7: case.BETA, 11: case.TP, 16: case.xMax, 17: case.yMax, 18: case.zMax,
-           53: case.GAMMA}
+           6: case.RM, 7: case.BETA, 11: case.TP, 12: case.TC, 13: case.XP, 14: case.YP, 15: case.ZP,
+           16: case.xMax, 17: case.yMax, 18: case.zMax, 52: case.QFH, 53: case.GAMMA, 54: case.HH}
     lines = "\n".join(f"    par[{k}] = {_hexf(v)};" for k, v in sorted(par.items()))
     return f"""#ifndef _3DMHD_SET_H_
 #define _3DMHD_SET_H_
@@ -150,18 +151,24 @@ def build(case: Case) -> Path:
     d = OUT_DIR / key
     exe = d / "ref_harness"
     harness = HERE / "ref_harness.cpp"
-    if exe.exists() and exe.stat().st_mtime >= harness.stat().st_mtime:
-        return exe
     d.mkdir(parents=True, exist_ok=True)
-    (d / "3dmhdparam.h").write_text(param_header(case))
-    (d / "3dmhdset.h").write_text(set_header(case))
-    shim = _shim_object()
-    cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-w",
-           "-I", str(d), "-I-", "-I", str(REF_DIR), "-I", str(HERE / "mpishim"),
-           str(harness), str(shim), "-o", str(exe)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("reference build failed:\n" + r.stderr[-4000:])
+    # one build per key at a time: concurrent builds would rewrite the
+    # generated headers under each other's compiler
+    with open(d / ".lock", "w") as lk:
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        if exe.exists() and exe.stat().st_mtime >= harness.stat().st_mtime:
+            return exe
+        (d / "3dmhdparam.h").write_text(param_header(case))
+        (d / "3dmhdset.h").write_text(set_header(case))
+        shim = _shim_object()
+        tmp = d / f"ref_harness.{os.getpid()}.tmp"
+        cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-w",
+               "-I", str(d), "-I-", "-I", str(REF_DIR), "-I", str(HERE / "mpishim"),
+               str(harness), str(shim), "-o", str(tmp)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference build failed:\n" + r.stderr[-4000:])
+        os.replace(tmp, exe)
     return exe
 
 
@@ -174,7 +181,8 @@ MODES = {"fluxes": 0, "steps": 1, "cfl": 2, "substage": 3, "dump": 4}
 def write_input(path: Path, case: Case, state: dict, mode: str, nsteps: int,
                 FT: np.ndarray | None = None, timt0: float = 0.0) -> None:
     m = metrics(case)
-    hdr = struct.pack("<8i8i", MAGIC, 1, case.nPx, case.nPy, case.nPz, int(case.lMag), MODES[mode], nsteps,
+    # version 2: the coordinate arrays EXX, WYY, ZEE follow the nine fields
+    hdr = struct.pack("<8i8i", MAGIC, 2, case.nPx, case.nPy, case.nPz, int(case.lMag), MODES[mode], nsteps,
                       *([0] * 8))
     hdr += struct.pack("<16d", case.dt, case.tb, timt0, *([0.0] * 13))
     with open(path, "wb") as f:
@@ -185,6 +193,8 @@ def write_input(path: Path, case: Case, state: dict, mode: str, nsteps: int,
             f.write(np.ascontiguousarray(state[k], dtype=np.float64).tobytes())
         ft = np.zeros(case.shape) if FT is None else FT
         f.write(np.ascontiguousarray(ft, dtype=np.float64).tobytes())
+        for a in coordinates(case):
+            f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
 
 
 def read_output(path: Path, case: Case, nsteps: int) -> dict:

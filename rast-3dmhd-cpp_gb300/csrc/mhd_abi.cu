@@ -104,9 +104,8 @@ int validate(const mhd_params* p, std::string& why) {
     if (p->ixCon != 0 || p->iyCon != 0) return why = "only periodic horizontal boundaries (ixCon=iyCon=0) exist in the reference", MHD_ERR_UNSUPPORTED;
     if (p->switches & MHD_SW_LREM) return why = "lRem (Rempel relaxation) is not built", MHD_ERR_UNSUPPORTED;
     if (p->izCon != 0 && p->izCon != 1) return why = "izCon must be 0 or 1", MHD_ERR_UNSUPPORTED;
-    if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 4) return why = "iTCon must be 0, 1 or 4", MHD_ERR_UNSUPPORTED;
-    if ((p->iTCon == 0 || p->iTCon == 1) && p->TP != 0.0)
-        return why = "the plume upper boundary (TP != 0 with iTCon 0/1) is not built", MHD_ERR_UNSUPPORTED;
+    if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 2 && p->iTCon != 4)
+        return why = "iTCon must be 0, 1, 2 or 4", MHD_ERR_UNSUPPORTED;
     if (p->iBCon != 0) return why = "iBCon must be 0", MHD_ERR_UNSUPPORTED;
     if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return why = "unknown precision", MHD_ERR_INVALID;
     if (p->precision == MHD_PREC_FP32 && p->path != MHD_PATH_FUSED)
@@ -351,7 +350,58 @@ int fused32_step(mhd_ctx* ctx, double dt) {
 
 }  // namespace
 
+int mhd_set_plume(mhd_ctx* ctx, const mhd_plume* pl) {
+    if (!ctx || !pl || !pl->EXX || !pl->WYY || !pl->ZEE) return MHD_ERR_INVALID;
+    if (!(pl->HH != 0.0)) return fail(ctx, MHD_ERR_INVALID, "HH must be non-zero");
+    const int nx = ctx->g.nx, ny = ctx->g.ny, nz = ctx->g.nz;
+    if (!ctx->d_plume) {
+        if (cudaMalloc(&ctx->d_plume, sizeof(double) * (size_t)(nx + ny + nz)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, MHD_ERR_NOMEM, "plume factor allocation failed");
+        }
+        ctx->bytes += sizeof(double) * (size_t)(nx + ny + nz);
+    }
+    // The reference's expressions (3dmhdsub.h:444-458,759-774): CLN uses the
+    // float overload of log (its C++ sees <math.h>'s std overloads), the top
+    // spot exp(CLN (x - XP)^2), the heat sink exp(CLN (x - XP)^2 / HH).
+    const double HH = pl->HH;
+    const double CLN = (double)(-4.0f * std::log(2.0f)) / HH / HH;
+    const bool sink = ctx->c.pl_mode == 3;
+    std::vector<double> h((size_t)(nx + ny + nz), 0.0);
+    auto sq = [](double v) { return v * v; };
+    for (int x = 0; x < nx; x++) h[x] = sink ? std::exp(CLN * sq(pl->EXX[x] - pl->XP) / HH) : std::exp(CLN * sq(pl->EXX[x] - pl->XP));
+    for (int y = 0; y < ny; y++) h[nx + y] = sink ? std::exp(CLN * sq(pl->WYY[y] - pl->YP) / HH) : std::exp(CLN * sq(pl->WYY[y] - pl->YP));
+    for (int z = 0; z < nz; z++) h[nx + ny + z] = std::exp(CLN * sq(pl->ZEE[z] - pl->ZP) / HH);
+    CK(cudaMemcpy(ctx->d_plume, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    ctx->c.plx = ctx->d_plume;
+    ctx->c.ply = ctx->d_plume + nx;
+    ctx->c.plz = ctx->d_plume + nx + ny;
+    ctx->c.pl_hh = HH;
+    ctx->pl_TP = ctx->prm.TP;
+    ctx->pl_TC = pl->TC;
+    ctx->pl_QFH = pl->QFH;
+    ctx->pl_OCV = ctx->k.OCV;
+    ctx->plume_set = true;
+    return ctxops::plume_update(ctx, ctx->timt);
+}
+
 namespace mhd::ctxops {
+bool plume_time_dependent(const mhd_ctx* c) { return c->c.pl_mode != 0 && c->pl_TC != 0.0; }
+int plume_update(mhd_ctx* ctx, double timt) {
+    if (ctx->c.pl_mode == 0) return MHD_OK;
+    if (!ctx->plume_set)
+        return fail(ctx, MHD_ERR_INVALID, "iTCon 2, or TP != 0 with iTCon 0/1, needs mhd_set_plume first");
+    const double TP = ctx->pl_TP, TC = ctx->pl_TC;
+    if (ctx->c.pl_mode == 3) {
+        // 3dmhdsub.h:446-458: TP * OCV [* 0.5 (1 + tanh(log 2 / QFH (TIMT - TC)))]
+        ctx->c.pl_s = (TC != 0.0) ? TP * ctx->pl_OCV * 0.5f * (1.0f + std::tanh(std::log(2.0f) / ctx->pl_QFH * (timt - TC)))
+                                  : TP * ctx->pl_OCV;
+    } else {
+        // 3dmhdsub.h:752-757
+        ctx->c.pl_tpr = (TC != 0.0) ? TP + (1.0f - TP) * std::exp(-timt / TC) : TP;
+    }
+    return MHD_OK;
+}
 FusedArgs fused_args(const mhd_ctx* ctx, int s, double dt, int in) {
     const double gam[3] = {ctx->k.GAM1, ctx->k.GAM2, ctx->k.GAM3};
     const double zet[3] = {ctx->k.ZETA1, ctx->k.ZETA2, 0.0};
@@ -511,6 +561,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     c.DDXmin = HUGE_VAL;
     for (int x = 1; x <= nx - 2; x++) c.DDXmin = (p.DDX[x] < c.DDXmin) ? p.DDX[x] : c.DDXmin;
     c.izCon = p.izCon; c.iTCon = p.iTCon; c.iBCon = p.iBCon;
+    // plume terms (their parameters come with mhd_set_plume)
+    c.pl_mode = (p.iTCon == 2) ? 3 : (p.TP != 0.0 && p.iTCon == 0) ? 1 : (p.TP != 0.0 && p.iTCon == 1) ? 2 : 0;
 
     ctx->red_blocks = 152 * 8;
     ctx->fp32 = p.precision == MHD_PREC_FP32;
@@ -567,6 +619,7 @@ int mhd_destroy(mhd_ctx* ctx) {
     cudaFree(ctx->U32[1]);
     cudaFree(ctx->FT64);
     cudaFree(ctx->d_bg);
+    cudaFree(ctx->d_plume);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -684,6 +737,7 @@ int mhd_fluxes(mhd_ctx* ctx) {
     if (!ctx) return MHD_ERR_INVALID;
     if (ctx->fp32) return fail(ctx, MHD_ERR_UNSUPPORTED, "the unfused calls work on FP64 state only");
     int rc = ensure_parity_buffers(ctx);
+    if (!rc) rc = ctxops::plume_update(ctx, ctx->timt);
     if (rc) return rc;
     double* S = ctx->Sb;
     ctx->ghosts_synced = false;  // 1/rho is written into RO over every cell, wall ghost planes included
@@ -712,6 +766,8 @@ int mhd_rk_gam(mhd_ctx* ctx, double coef) { return rk(ctx, 2, coef); }
 int mhd_bcon(mhd_ctx* ctx, double timt) {
     if (!ctx) return MHD_ERR_INVALID;
     if (ctx->fp32) return fail(ctx, MHD_ERR_UNSUPPORTED, "the unfused calls work on FP64 state only");
+    const int rc = ctxops::plume_update(ctx, timt);
+    if (rc) return rc;
     const int e = parity_bcon(ctx->sw, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), timt, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "BCON launch");
     return MHD_OK;
@@ -775,6 +831,8 @@ int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out) {
         if (rc) return rc;
         if (dt < 1.0e-8f) return fail(ctx, MHD_ERR_DT_TOO_SMALL, "DT too small, halt (3dmhd.cpp:292-331)");
     }
+    rc = ctxops::plume_update(ctx, ctx->timt);
+    if (rc) return rc;
     rc = ctx->fp32 ? fused32_step(ctx, dt) : ctx->prm.path == MHD_PATH_PARITY ? parity_step(ctx, dt) : fused_step(ctx, dt);
     if (rc) return rc;
     ctxops::advance_time(ctx, dt);
@@ -800,8 +858,9 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt) {
 int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out) {
     if (!ctx || n < 0) return MHD_ERR_INVALID;
     if (out) memset(out, 0, sizeof(*out));
-    if (ctx->fp32 || ctx->prm.path == MHD_PATH_PARITY) {
-        // these paths read the CFL dt back every step
+    if (ctx->fp32 || ctx->prm.path == MHD_PATH_PARITY || ctxops::plume_time_dependent(ctx)) {
+        // these paths read the CFL dt back every step (a time-dependent plume
+        // needs TIMT on the host before each step)
         mhd_diag d{};
         for (int s = 0; s < n; s++) {
             const int rc = mhd_step(ctx, 0.0, &d);
@@ -810,6 +869,7 @@ int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out) {
         }
         return MHD_OK;
     }
+    if (int rp = ctxops::plume_update(ctx, ctx->timt)) return rp;
     double* rec = ctx->d_out + 8;
     double* h = ctx->h_out + 8;
     for (int k = 0; k < kDtRecord; k++) h[k] = 0.0;

@@ -371,6 +371,11 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
             fprintf(stderr, "mhd_batch_create: instances must be fused-path contexts\n");
             return MHD_ERR_UNSUPPORTED;
         }
+        if (c->c.pl_mode != 0 && (!c->plume_set || ctxops::plume_time_dependent(c))) {
+            delete b;
+            fprintf(stderr, "mhd_batch_create: plume terms must be set and time-independent (TC = 0) in a batch\n");
+            return MHD_ERR_UNSUPPORTED;
+        }
         if (i > 0 && (c->sw != b->sw || c->fp32 != b->fp32)) {
             delete b;
             fprintf(stderr, "mhd_batch_create: all instances of a batch need the same switch set\n");

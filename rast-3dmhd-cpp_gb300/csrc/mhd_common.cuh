@@ -44,6 +44,14 @@ struct Consts {
     double hx, h2x, hy, h2y, hz, h2z;
     double GRAV, THETA, RE, REPR, ORE, OCV, CV, GAMMA, OMX, OMZ, RM, ORM, OBETA, TB, TP, SFF;
     double DDXmin;  // min of DDX over interior x (NaN skipped), for the CFL reduction
+    // Plume terms (3dmhdsub.h:443-459,750-778): pl_mode 0 none, 1 cooling spot
+    // on the top wall with iTCon 0, 2 the same with iTCon 1, 3 internal heat
+    // sink (iTCon 2).  plx/ply/plz are the host-computed Gaussian factors per
+    // x, y, z; pl_tpr (top spot) and pl_s (sink amplitude) depend on TIMT and
+    // are refreshed by the host before every step.
+    int pl_mode, pl_pad_;
+    const double *plx, *ply, *plz;
+    double pl_hh, pl_tpr, pl_s;
     int izCon, iTCon, iBCon, pad_;
     const double *dxxdx, *d2xxdx2, *DDX;
     const double *dyydy, *d2yydy2, *DDY;

@@ -52,6 +52,10 @@ struct mhd_ctx {
     bool profiling = false;
     std::vector<cudaEvent_t> prof_events;  // pairs around each substage launch
     size_t prof_used = 0;
+    // plume terms: parameters from mhd_set_plume, Gaussian factors on the device
+    bool plume_set = false;
+    double pl_TP = 0.0, pl_TC = 0.0, pl_QFH = 0.0, pl_OCV = 0.0;
+    double* d_plume = nullptr;  // plx (nx), ply (ny), plz (nz)
     // host-to-host steps: copy streams and per-slab events (created on first use)
     cudaStream_t s_up = nullptr, s_down = nullptr;
     std::vector<cudaEvent_t> slab_events;
@@ -68,6 +72,11 @@ Fields8 fields_of(const mhd_ctx* c, double* base);
 int fail(mhd_ctx* c, int code, const std::string& msg);
 // one completed step of length dt: nIt, TIMC and TIMT advance as 3dmhdsub.h:150-152
 void advance_time(mhd_ctx* c, double dt);
+// refresh the time-dependent plume scalars for simulation time timt; fails
+// when the context needs plume parameters that mhd_set_plume has not given
+int plume_update(mhd_ctx* c, double timt);
+// whether the plume terms depend on the simulation time (TC != 0)
+bool plume_time_dependent(const mhd_ctx* c);
 // FusedArgs of substage s (0..2) of the fused FP64 step reading state buffer
 // U[in] and writing U[1-in]
 FusedArgs fused_args(const mhd_ctx* c, int s, double dt, int in);

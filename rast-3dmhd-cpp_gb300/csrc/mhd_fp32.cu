@@ -203,6 +203,9 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 const float lapT = D2x(F_DT) + D2y(F_DT) + (a.zf[4 * nzz + z] + D2z(F_DT));
                 ft = fmaf(ri * tmpc, fmaf(a.zf[5 * nzz + z], lapT, a.zf[6 * nzz + z] * Tz), ft);
             }
+            // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
+            if (c.pl_mode == 3)
+                ft = fmaf(-(float)c.pl_s * ri, (float)(c.plx[x] * c.ply[y] * c.plz[z]), ft);
 
             // ---- viscous Laplacians and cross terms
             fu = fmaf(ore43, D2x(F_U), fmaf(ore, D2y(F_U) + D2z(F_U), fu));
@@ -371,7 +374,14 @@ __device__ __forceinline__ void bcon32_cell(const Grid& g, const Consts& c, cons
         rv = ro * (c.C43 * (double)RV[i1] / ro1 - c.C13 * (double)RV[i2] / ro2);
     }
     if (wall == 0) {
-        if (c.iTCon == 1) {
+        if (c.pl_mode == 1) {
+            // cooling spot on the top wall (3dmhdsub.h:750-766)
+            tt = 1.0f - (1.0f - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh;
+        } else if (c.pl_mode == 2) {
+            const double DZ = 1.0f / (double)(g.nPz - 1) / c.dzzdz[z];
+            tt = c.C43 * t1 - c.C13 * t2 -
+                 c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
+        } else if (c.iTCon == 1) {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
             tt = c.C43 * t1 - c.C13 * t2 - c.C23 * DZ * c.THETA;
         } else {

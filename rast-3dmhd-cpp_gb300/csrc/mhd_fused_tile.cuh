@@ -233,6 +233,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
                 ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
             }
+            // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
+            if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
 
             // ---- viscous Laplacians (3dmhdsub.h:462-472)
             fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
@@ -371,7 +373,14 @@ __device__ __forceinline__ void bcon_cell(const Grid& g, const Consts& c, const 
         rv = RO[i] * (c.C43 * RV[i1] / RO[i1] - c.C13 * RV[i2] / RO[i2]);
     }
     if (wall == 0) {
-        if (c.iTCon == 1) {
+        if (c.pl_mode == 1) {
+            // cooling spot on the top wall (3dmhdsub.h:750-766)
+            tt = 1.0f - (1.0f - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh;
+        } else if (c.pl_mode == 2) {
+            const double DZ = 1.0f / (double)(g.nPz - 1) / c.dzzdz[z];
+            tt = c.C43 * TT[i1] - c.C13 * TT[i2] -
+                 c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
+        } else if (c.iTCon == 1) {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
             tt = c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA;
         } else {

@@ -157,6 +157,8 @@ __global__ void k_flux(Grid g, Consts c, Fields8 U, Fields8 F, const double* __r
         ft += ((d2y(TT, i, sy, y, c) * ri) * c.RKAPA[z]) * tmp;
         ft += ((d2z(TT, i, sz, z, c) * ri) * c.RKAPA[z]) * tmp;
         ft += ((d1z(TT, i, sz, z, c) * ri) * c.DKAPA[z]) * tmp;
+        // internal plume heat sink (iTCon 2), 3dmhdsub.h:443-459
+        if (c.pl_mode == 3) ft -= (((c.pl_s * ri) * c.plx[x]) * c.ply[y]) * c.plz[z];
 
         // viscous Laplacians, 3dmhdsub.h:462-472
         fu += d2x(UU, i, x, c) * (c.ORE * c.C43);
@@ -388,7 +390,15 @@ __global__ void k_bcon(Grid g, Consts c, Fields8 U, double timt) {
         RV[i] = RO[i] * (c.C43 * RV[i + sz] / RO[i + sz] - c.C13 * RV[i + 2 * sz] / RO[i + 2 * sz]);
     }
     RW[i] = 0.0f;
-    if (c.iTCon == 1) {
+    if (c.pl_mode == 1) {
+        // cooling spot on the top wall, 3dmhdsub.h:750-766
+        TT[i] = 1.0f - (1.0f - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh;
+    } else if (c.pl_mode == 2) {
+        // the same with the fixed-flux wall, 3dmhdsub.h:767-777 (DZ in double here)
+        const double DZ = 1.0f / (double)(g.nPz - 1) / c.dzzdz[zl];
+        TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] -
+                c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
+    } else if (c.iTCon == 1) {
         const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[zl];
         TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] - c.C23 * DZ * c.THETA;
     } else {

@@ -78,6 +78,7 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
     }
     int rc = ctxops::ensure_u1(ctx);
     if (!rc && (ctx->sw & kSwShr)) rc = ctxops::alloc_block(ctx, &ctx->Fb, 8);
+    if (!rc) rc = ctxops::plume_update(ctx, ctx->timt);
     if (rc) return rc;
     if (!ctx->s_up) {
         PCK(cudaStreamCreateWithFlags(&ctx->s_up, cudaStreamNonBlocking));

@@ -56,6 +56,11 @@ class MhdDiag(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class MhdPlume(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("XP", "YP", "ZP", "HH", "TC", "QFH")] + \
+               [(n, C.POINTER(C.c_double)) for n in ("EXX", "WYY", "ZEE")]
+
+
 NOALLOC_MAX_CELLS = 393216
 
 
@@ -103,6 +108,7 @@ SIGNATURES = {
     "mhd_steps": [C.c_void_p, C.c_int, C.c_double],
     "mhd_steps_cfl": [C.c_void_p, C.c_int, C.POINTER(MhdDiag)],
     "mhd_step_host": [C.c_void_p, _DP, _DP, C.c_double],
+    "mhd_set_plume": [C.c_void_p, C.POINTER(MhdPlume)],
     "mhd_selftest_convert": [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],

@@ -53,6 +53,15 @@ class Case:
     RM: float = 100.0
     BETA: float = 2.0
     TP: float = 0.0
+    # plume: top-boundary cooling spot (TP != 0, iTCon 0/1) and internal heat
+    # source (iTCon 2) at (XP, YP, ZP), width HH, time scales TC, QFH
+    # (3dmhd.cpp:413-426; 3dmhdsub.h:443-459,750-778)
+    XP: float = 0.0
+    YP: float = 0.0
+    ZP: float = 0.0
+    HH: float = 0.0
+    TC: float = 0.0
+    QFH: float = 0.0
     xMax: float = 6.0
     yMax: float = 6.0
     zMax: float = 2.0
@@ -142,6 +151,14 @@ def tanh_metric(n_interior: int, umax: float, s: float):
     dd = orx * (1.0 / dxidu)
     pad = lambda v: np.concatenate([[v[0]], v, [v[-1]]])
     return pad(dxidu), pad(d2xidu2), pad(dd)
+
+
+def coordinates(case: Case) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """EXX, WYY, ZEE: the x, y, z coordinates of every index (x and y
+    uniform, extended linearly into the ghosts; z from z_coordinate)."""
+    x = case.xMax * (np.arange(case.nx, dtype=np.float64) - 1.0) / (case.nPx - 1)
+    y = case.yMax * (np.arange(case.ny, dtype=np.float64) - 1.0) / (case.nPy - 1)
+    return x, y, z_coordinate(case)
 
 
 def z_coordinate(case: Case) -> np.ndarray:
@@ -279,6 +296,20 @@ def small_cases() -> dict[str, Case]:
         "hydro_default_bc": Case(name="hydro_default_bc", lMag=False, izCon=1, iTCon=4, TP=f32(0.1), **base),
         "mhd_rot_flux": Case(name="mhd_rot_flux", lRot=True, ANG=0.3, izCon=1, iTCon=1, **base),
         "hydro_shr": Case(name="hydro_shr", lMag=False, lShr=True, izCon=0, iTCon=4, TP=f32(0.1), **base),
+    }
+
+
+def plume_cases() -> dict[str, Case]:
+    """Cases with the plume terms: the cooling spot on the top wall (TP != 0
+    with iTCon 0, time-dependent through TC, and with iTCon 1) and the
+    internal heat sink (iTCon 2, time-dependent through TC and QFH)."""
+    base = dict(nPx=12, nPy=8, nPz=8, nPEy=2, nPEz=2, seed=7, noise=1e-2, bz0=1e-2, dt=2e-4,
+                XP=3.0, YP=3.0, HH=1.5)
+    return {
+        "plume_top0": Case(name="plume_top0", iTCon=0, TP=0.4, TC=0.01, **base),
+        "plume_top1": Case(name="plume_top1", lMag=False, iTCon=1, izCon=1, TP=0.3, **base),
+        "plume_src2": Case(name="plume_src2", lRot=True, iTCon=2, TP=2.0, TC=1e-4, QFH=2e-4,
+                           **dict(base, HH=1.0, ZP=1.0)),
     }
 
 

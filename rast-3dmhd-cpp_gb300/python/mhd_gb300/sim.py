@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 
 from . import abi
-from .case import Case, STATE_FIELDS, metrics
+from .case import Case, STATE_FIELDS, coordinates, metrics
 
 
 def params_for(case: Case, path: str = "fused", precision: str = "fp64") -> tuple[abi.MhdParams, list]:
@@ -58,6 +58,8 @@ class Simulation:
         if st != abi.MHD_OK:
             raise abi.MhdError(st, "mhd_create failed")
         self.ctx = ctx
+        if case.iTCon == 2 or (case.TP != 0.0 and case.iTCon in (0, 1)):
+            self.set_plume()
         self._keep = keep
         self.timt = 0.0
 
@@ -116,6 +118,15 @@ class Simulation:
     def set_time(self, timt: float, nit: int = 0) -> None:
         self.timt = timt
         self._ck(self.L.mhd_set_time(self.ctx, timt, nit))
+
+    def set_plume(self) -> None:
+        """Plume parameters and coordinates of the case (mhd_set_plume)."""
+        self._plume_coords = [np.ascontiguousarray(a, dtype=np.float64) for a in coordinates(self.case)]
+        pl = abi.MhdPlume()
+        for k in ("XP", "YP", "ZP", "HH", "TC", "QFH"):
+            setattr(pl, k, float(getattr(self.case, k)))
+        pl.EXX, pl.WYY, pl.ZEE = (_dp(a) for a in self._plume_coords)
+        self._ck(self.L.mhd_set_plume(self.ctx, C.byref(pl)))
 
     # ---- the reference's entry points ---------------------------------------
     def fluxes(self) -> None:

@@ -49,8 +49,8 @@ def test_status_strings(lib):
 @pytest.mark.parametrize("change, status", [
     (dict(nPz=3), -1),
     (dict(izCon=2), -2),
-    (dict(iTCon=2), -2),
-    (dict(TP=0.1, iTCon=0), -2),
+    (dict(iTCon=3), -2),
+    (dict(iBCon=1), -2),
     (dict(RE=0.0), -1),
 ])
 def test_invalid_configs_rejected_without_gpu(lib, change, status):
