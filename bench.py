@@ -509,8 +509,11 @@ def run_serve(args, dist: Dist) -> None:
     n = args.serve_requests
     smin, smax = max(1, 50 // args.serve_step_scale), max(2, 2000 // args.serve_step_scale)
     reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
-    srv = Server(150 << 30, quantum=25)
+    srv = Server(150 << 30, quantum=25, policy="srpt")
     st = srv.run(reqs, realtime=True)
+    # the same stream admitted first come, first served (everything resident shares the GPU)
+    fifo_reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
+    fifo = Server(150 << 30, quantum=25, policy="fifo", tile=st["tile"]).run(fifo_reqs, realtime=True)
     # baseline: the same requests one after another on the plain FP64 path
     serial_reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
     base = run_serial(serial_reqs)
@@ -518,7 +521,10 @@ def run_serve(args, dist: Dist) -> None:
            "steps_range": [smin, smax], "hbm_budget_gb": 150,
            "value": st["value"], "wall_s": st["wall_s"], "tts_p50_s": st["tts_p50_s"],
            "tts_p99_s": st["tts_p99_s"], "max_resident": st["max_resident"], "tile": st["tile"],
-           "batch_rebuilds": st["batch_rebuilds"],
+           "batch_rebuilds": st["batch_rebuilds"], "policy": st["policy"],
+           "target_cells": srv.target_cells,
+           "fifo": {k: fifo[k] for k in ("value", "wall_s", "tts_p50_s", "tts_p99_s", "max_resident",
+                                          "batch_rebuilds")},
            "serial_plain_fp64": base, "throughput_vs_serial": st["value"] / base["value"],
            "config": {"workload": f"Poisson stream of {n} simulations at 20/s, grids log-uniform 32^3..256^2x128, "
                                   f"steps uniform [{smin},{smax}] (the configured [50,2000] / "

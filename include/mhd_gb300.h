@@ -79,7 +79,10 @@ typedef struct mhd_params {
     int path;
     int reserved_i[5];
     double RE, PR, THETA, GRAV, RY, ANG, RM, BETA, TP, GAMMA, SFF, TB;
-    double reserved_d[4];
+    /* with MHD_SW_LREM: the wall values of the static model (Static(),
+     * 3dmhdphsic.h:592-594) used by BCON (3dmhdsub.h:783-802,852-854) */
+    double TU, DZTU, DZTB;
+    double reserved_d[1];
     const double *dxxdx, *d2xxdx2, *DDX;
     const double *dyydy, *d2yydy2, *DDY;
     const double *dzzdz, *d2zzdz2, *DDZ;

@@ -18,6 +18,7 @@
 #include "mhd_oracle.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -140,6 +141,14 @@ int orc_fluxes(const orc_params* p, orc_fields* f) {
     }
     SWEEP(R_, FR[i] -= WW1[i]);
 
+    /* lRem: the wall ghost planes of RO take the second interior plane,
+     * 3dmhdsub.h:229-238 (the horizontal mean computed after it there is
+     * only used with iD != 0) */
+    if (p->lRem) {
+        memcpy(RO, RO + 2 * sz, sizeof(double) * sz);
+        memcpy(RO + (size_t)(nz - 1) * sz, RO + (size_t)(nz - 3) * sz, sizeof(double) * sz);
+    }
+
     /* pressure, gravity and 1/rho in place, 3dmhdsub.h:266-272 */
     SWEEP(R_, FW[i] = RO[i] * p->GRAV);
     SWEEP(EXT_, WW1[i] = RO[i] * TT[i]);
@@ -163,18 +172,46 @@ int orc_fluxes(const orc_params* p, orc_fields* f) {
     SWEEP(R_, FW[i] -= MDZ(RW, WW));
 
     /* temperature advection, 3dmhdsub.h:293-296 */
+    double* TTM = NULL;
     if (!p->lShr) {
         SWEEP(R_, FT[i] = -(D1X(TT) * UU[i]));
         SWEEP(R_, FT[i] -= D1Y(TT) * VV[i]);
         SWEEP(R_, FT[i] -= D1Z(TT) * WW[i]);
+        if (p->lRem) {
+            /* horizontal_mean (3dmhdsub.h:698-718, one y rank) and WW1 = TT - TTM */
+            TTM = (double*)calloc((size_t)nz, sizeof(double));
+            for (int z = 0; z < nz; z++) {
+                double w = 0;
+                for (int y = 1; y < ny - 1; y++)
+                    for (int x = 1; x < nx - 1; x++) w += TT[((size_t)z * ny + y) * nx + x];
+                TTM[z] = w / (float)((nx - 2) * (ny - 2));
+            }
+            SWEEP(EXT_, WW1[i] = TT[i] - TTM[z]);
+        }
     }
 
-    /* conduction, 3dmhdsub.h:315-319 */
     tmp = p->OCV / p->REPR;
-    SWEEP(R_, FT[i] += ((D2X(TT) * RO[i]) * p->RKAPA[z]) * tmp);
-    SWEEP(R_, FT[i] += ((D2Y(TT) * RO[i]) * p->RKAPA[z]) * tmp);
-    SWEEP(R_, FT[i] += ((D2Z(TT) * RO[i]) * p->RKAPA[z]) * tmp);
-    SWEEP(R_, FT[i] += ((D1Z(TT) * RO[i]) * p->DKAPA[z]) * tmp);
+    if (p->lRem && TTM) {
+        /* conduction of the deviation plus the mean profile's, 3dmhdsub.h:304-313 */
+        SWEEP(R_, FT[i] += (D2X(WW1) * RO[i]) * tmp);
+        SWEEP(R_, FT[i] += (D2Y(WW1) * RO[i]) * tmp);
+        SWEEP(R_, FT[i] += (D2Z(WW1) * RO[i]) * tmp);
+        double* HRAD = (double*)calloc((size_t)nz, sizeof(double));
+        for (int z = zl; z < zr; z++) {
+            HRAD[z] = (((TTM[z + 1] - 2.0f * TTM[z] + TTM[z - 1])) * p->h2z * p->dzzdz[z] * p->dzzdz[z] +
+                       (TTM[z + 1] - TTM[z - 1]) * p->hz * p->d2zzdz2[z]) * p->RKAPA[z];
+            HRAD[z] += (TTM[z + 1] - TTM[z - 1]) * p->hz * p->dzzdz[z] * p->DKAPA[z];
+        }
+        SWEEP(R_, FT[i] += (RO[i] * HRAD[z]) * tmp);
+        free(HRAD);
+    } else {
+        /* conduction, 3dmhdsub.h:315-319 */
+        SWEEP(R_, FT[i] += ((D2X(TT) * RO[i]) * p->RKAPA[z]) * tmp);
+        SWEEP(R_, FT[i] += ((D2Y(TT) * RO[i]) * p->RKAPA[z]) * tmp);
+        SWEEP(R_, FT[i] += ((D2Z(TT) * RO[i]) * p->RKAPA[z]) * tmp);
+        SWEEP(R_, FT[i] += ((D1Z(TT) * RO[i]) * p->DKAPA[z]) * tmp);
+    }
+    free(TTM);
 
     /* internal plume heat sink (iTCon 2), 3dmhdsub.h:443-459; RO holds 1/rho.
      * log(2.0f) is the float overload in the reference's C++ (3dmhdphsic.h
@@ -448,7 +485,13 @@ int orc_bcon(const orc_params* p, orc_fields* f, double timt) {
         }
     } else if (p->iTCon == 0 || p->iTCon == 2 || p->iTCon == 4) {
         const int is4 = p->iTCon == 4;
-        SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, TT[i] = 1.0f; if (is4 && x < nx / 2) TT[i] = 1.0f - p->TP);
+        if (p->lRem) {
+            SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, TT[i] = p->TU);
+        } else {
+            SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, TT[i] = 1.0f; if (is4 && x < nx / 2) TT[i] = 1.0f - p->TP);
+        }
+    } else if (p->lRem) { /* iTCon == 1, lRem: 3dmhdsub.h:800-802 */
+        SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1, TT[i] = p->C43 * TT[i + sz] - p->C13 * TT[i + 2 * sz] + p->DZTU);
     } else { /* iTCon == 1 with TP == 0: fixed flux */
         const double DZ = 1.0f / (float)(p->nPz - 1) / p->dzzdz[zl];
         SWEEP(zl, zl + 1, 1, ny - 1, 1, nx - 1,
@@ -467,6 +510,8 @@ int orc_bcon(const orc_params* p, orc_fields* f, double timt) {
     SWEEP(zr - 1, zr, 1, ny - 1, 1, nx - 1, RW[i] = 0.0f);
     if (p->izCon == 0) {
         SWEEP(zr - 1, zr, 1, ny - 1, 1, nx - 1, TT[i] = p->TB);
+    } else if (p->lRem) { /* 3dmhdsub.h:852-854 */
+        SWEEP(zr - 1, zr, 1, ny - 1, 1, nx - 1, TT[i] = p->C43 * TT[i - sz] - p->C13 * TT[i - 2 * sz] + p->DZTB);
     } else {
         const double DZ = 1.0f / (float)(p->nPz - 1) / p->dzzdz[zr - 1];
         SWEEP(zr - 1, zr, 1, ny - 1, 1, nx - 1,
@@ -522,7 +567,8 @@ double orc_cfl_dt(const orc_params* p, orc_fields* f, double* umach) {
                 double DD = dmin(p->DDY[y], p->DDZ[z]);
                 if (nx > 3) DD = dmin(DD, p->DDX[x]);
                 w0 = dmin(w0, DD / sqrt(UU));
-                w1 = dmin(w1, 0.5f * DD * DD * p->REPR * p->CV * RO[i] / p->RKAPA[z]);
+                w1 = dmin(w1, p->lRem ? 0.5f * DD * DD * p->REPR * p->CV * RO[i] / (1.0f + p->RKAPA[z])
+                                      : 0.5f * DD * DD * p->REPR * p->CV * RO[i] / p->RKAPA[z]);
                 w2 = dmin(w2, 0.375f * DD * DD * p->RE * RO[i]);
                 if (p->lMag) w3 = dmin(w3, 0.5f * DD * DD * p->RM);
             }

@@ -41,6 +41,10 @@ typedef struct orc_params {
     const double *EXX, *WYY, *ZEE;
     double XP, YP, ZP, HH, TC, QFH;
     double TIMT;
+    /* lRem (Rempel relaxation; 3dmhdsub.h:229-242,297-313,783-802,852-854):
+     * switch and the static model's TU, DZTU, DZTB (3dmhdphsic.h:592-594) */
+    int lRem, pad2_;
+    double TU, DZTU, DZTB;
 } orc_params;
 
 /* Field slots.  0-7 state, 8-15 right-hand sides, 16-23 RK register,

@@ -52,7 +52,9 @@ class OrcParams(C.Structure):
                [(n, C.POINTER(C.c_double)) for n in ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY",
                                                       "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")] + \
                [(n, C.POINTER(C.c_double)) for n in ("EXX", "WYY", "ZEE")] + \
-               [(n, C.c_double) for n in ("XP", "YP", "ZP", "HH", "TC", "QFH", "TIMT")]
+               [(n, C.c_double) for n in ("XP", "YP", "ZP", "HH", "TC", "QFH", "TIMT")] + \
+               [("lRem", C.c_int), ("pad2_", C.c_int)] + \
+               [(n, C.c_double) for n in ("TU", "DZTU", "DZTB")]
 
 
 class OrcFields(C.Structure):
@@ -110,8 +112,9 @@ class OracleSim:
         self._coord_arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in coordinates(case)]
         for n, a in zip(("EXX", "WYY", "ZEE"), self._coord_arrays):
             setattr(p, n, _dptr(a))
-        for k in ("XP", "YP", "ZP", "HH", "TC", "QFH"):
+        for k in ("XP", "YP", "ZP", "HH", "TC", "QFH", "TU", "DZTU", "DZTB"):
             setattr(p, k, float(getattr(case, k)))
+        p.lRem = int(case.lRem)
         self.L.orc_set_constants(C.byref(p), case.nPx, case.nPy, case.nPz)
         self.p = p
         self.f = OrcFields()

@@ -200,6 +200,12 @@ int main(int argc, char** argv) {
         load_field(g_fields + (size_t)f * nglob, *fields_in[f]);
     }
     TB = h.TB;
+#if lRem
+    /* Static() derives these from its model (3dmhdphsic.h:592-594); the input gives them */
+    TU = h.reserved[0];
+    DZTU = h.reserved[1];
+    DZTB = h.reserved[2];
+#endif
     TIMI = h.TIMT0;
     TIMC = 0.0;
     TIMT = TIMI;

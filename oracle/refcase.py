@@ -67,7 +67,7 @@ const std::string fOut = outputDir + "test";
 #define lRot {_b(case.lRot)}
 #define lMag {_b(case.lMag)}
 #define lPot false
-#define lRem false
+#define lRem {_b(case.lRem)}
 #define lShr {_b(case.lShr)}
 const int nPEy = {case.nPEy};
 const int nPEz = {case.nPEz};
@@ -184,7 +184,8 @@ def write_input(path: Path, case: Case, state: dict, mode: str, nsteps: int,
     # version 2: the coordinate arrays EXX, WYY, ZEE follow the nine fields
     hdr = struct.pack("<8i8i", MAGIC, 2, case.nPx, case.nPy, case.nPz, int(case.lMag), MODES[mode], nsteps,
                       *([0] * 8))
-    hdr += struct.pack("<16d", case.dt, case.tb, timt0, *([0.0] * 13))
+    # reserved doubles 0-2: the lRem wall values TU, DZTU, DZTB
+    hdr += struct.pack("<16d", case.dt, case.tb, timt0, case.TU, case.DZTU, case.DZTB, *([0.0] * 10))
     with open(path, "wb") as f:
         f.write(hdr)
         for a in m.arrays():

@@ -102,7 +102,11 @@ int validate(const mhd_params* p, std::string& why) {
     const double cells = (double)(p->nPx + 2) * (p->nPy + 2) * (p->nPz + 2);
     if (cells > 2.0e9) return why = "grid too large for 32-bit plane indexing", MHD_ERR_INVALID;
     if (p->ixCon != 0 || p->iyCon != 0) return why = "only periodic horizontal boundaries (ixCon=iyCon=0) exist in the reference", MHD_ERR_UNSUPPORTED;
-    if (p->switches & MHD_SW_LREM) return why = "lRem (Rempel relaxation) is not built", MHD_ERR_UNSUPPORTED;
+    if ((p->switches & MHD_SW_LREM) && (p->switches & MHD_SW_LSHR))
+        return why = "lRem with lShr: the reference's temperature terms then read arrays it did not fill this call (3dmhdsub.h:292-313)",
+               MHD_ERR_UNSUPPORTED;
+    if ((p->switches & MHD_SW_LREM) && p->precision == MHD_PREC_FP32)
+        return why = "lRem runs on FP64 contexts only", MHD_ERR_UNSUPPORTED;
     if (p->izCon != 0 && p->izCon != 1) return why = "izCon must be 0 or 1", MHD_ERR_UNSUPPORTED;
     if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 2 && p->iTCon != 4)
         return why = "iTCon must be 0, 1, 2 or 4", MHD_ERR_UNSUPPORTED;
@@ -167,6 +171,11 @@ int fused_step(mhd_ctx* ctx, double dt, const double* dtp = nullptr) {
     for (int s = 0; s < 3; s++) {
         FusedArgs a = ctxops::fused_args(ctx, s, dt, ctx->cur);
         a.dtp = dtp;
+        if (ctx->c.lrem) {
+            // horizontal means of the substage's input T (3dmhdsub.h:297-313)
+            const int e = lrem_profiles(ctx->g, ctx->c, a.U.p[S_TT], ctx->d_lrem, false, ctx->stream);
+            if (e) return cuda_fail(ctx, (cudaError_t)e, "lRem profiles launch");
+        }
         cudaEvent_t* ev = nullptr;
         if (ctx->profiling) {
             if (ctx->prof_used + 2 > ctx->prof_events.size()) {
@@ -561,6 +570,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     c.DDXmin = HUGE_VAL;
     for (int x = 1; x <= nx - 2; x++) c.DDXmin = (p.DDX[x] < c.DDXmin) ? p.DDX[x] : c.DDXmin;
     c.izCon = p.izCon; c.iTCon = p.iTCon; c.iBCon = p.iBCon;
+    c.lrem = (p.switches & MHD_SW_LREM) ? 1 : 0;
+    c.TU = p.TU; c.DZTU = p.DZTU; c.DZTB = p.DZTB;
     // plume terms (their parameters come with mhd_set_plume)
     c.pl_mode = (p.iTCon == 2) ? 3 : (p.TP != 0.0 && p.iTCon == 0) ? 1 : (p.TP != 0.0 && p.iTCon == 1) ? 2 : 0;
 
@@ -588,6 +599,15 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     if (!arc) arc = alloc_block(ctx, &ctx->Zb, 8);
     if (!arc && ctx->fp32 && (ctx->sw & kSwShr)) arc = alloc_block(ctx, &ctx->FT64, 1);
     if (!arc && cudaMalloc(&ctx->red, sizeof(double) * 8 * (size_t)ctx->red_blocks) != cudaSuccess) arc = MHD_ERR_NOMEM;
+    if (!arc && c.lrem) {
+        if (cudaMalloc(&ctx->d_lrem, sizeof(double) * 3 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
+        else {
+            ctx->bytes += sizeof(double) * 3 * nz;
+            c.lrem_ttm = ctx->d_lrem;
+            c.lrem_hrad = ctx->d_lrem + nz;
+            c.lrem_g = ctx->d_lrem + 2 * nz;
+        }
+    }
     // d_out: 8 doubles of reduction results, then the kDtRecord-double time-step record
     if (!arc && cudaMalloc(&ctx->d_out, sizeof(double) * (8 + kDtRecord)) != cudaSuccess) arc = MHD_ERR_NOMEM;
     if (!arc && cudaMallocHost(&ctx->h_out, sizeof(double) * (8 + kDtRecord)) != cudaSuccess) arc = MHD_ERR_NOMEM;
@@ -620,6 +640,7 @@ int mhd_destroy(mhd_ctx* ctx) {
     cudaFree(ctx->FT64);
     cudaFree(ctx->d_bg);
     cudaFree(ctx->d_plume);
+    cudaFree(ctx->d_lrem);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -739,6 +760,19 @@ int mhd_fluxes(mhd_ctx* ctx) {
     int rc = ensure_parity_buffers(ctx);
     if (!rc) rc = ctxops::plume_update(ctx, ctx->timt);
     if (rc) return rc;
+    if (ctx->c.lrem) {
+        // lRem: the wall ghost planes of RO take the second interior plane
+        // (3dmhdsub.h:229-238), and the horizontal means of T in the
+        // reference's summation order (3dmhdsub.h:297-301,698-718)
+        double* RO = ctx->U[ctx->cur] + (size_t)S_RO * ctx->ncell;
+        const size_t plane = (size_t)ctx->g.sz;
+        CK(cudaMemcpyAsync(RO, RO + 2 * plane, plane * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(RO + (size_t)(ctx->g.nz - 1) * plane, RO + (size_t)(ctx->g.nz - 3) * plane,
+                           plane * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        const int e = lrem_profiles(ctx->g, ctx->c, ctx->U[ctx->cur] + (size_t)S_TT * ctx->ncell, ctx->d_lrem, true,
+                                    ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "lRem profiles launch");
+    }
     double* S = ctx->Sb;
     ctx->ghosts_synced = false;  // 1/rho is written into RO over every cell, wall ghost planes included
     const int e = parity_fluxes(ctx->sw, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), fields_of(ctx, ctx->Fb), S,

@@ -371,6 +371,11 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
             fprintf(stderr, "mhd_batch_create: instances must be fused-path contexts\n");
             return MHD_ERR_UNSUPPORTED;
         }
+        if (c->c.lrem) {
+            delete b;
+            fprintf(stderr, "mhd_batch_create: lRem instances step alone (per-substage plane means)\n");
+            return MHD_ERR_UNSUPPORTED;
+        }
         if (c->c.pl_mode != 0 && (!c->plume_set || ctxops::plume_time_dependent(c))) {
             delete b;
             fprintf(stderr, "mhd_batch_create: plume terms must be set and time-independent (TC = 0) in a batch\n");

@@ -52,6 +52,13 @@ struct Consts {
     int pl_mode, pl_pad_;
     const double *plx, *ply, *plz;
     double pl_hh, pl_tpr, pl_s;
+    // lRem (3dmhdsub.h:229-238,297-313,783-802,852-854): per-substage arrays
+    // filled before the right-hand side: lrem_ttm = horizontal mean of T per
+    // z, lrem_hrad = HRAD, lrem_g = HRAD minus the z second derivative of the
+    // mean (the fused kernels' form); TU, DZTU, DZTB for BCON
+    int lrem, lrem_pad_;
+    const double *lrem_ttm, *lrem_hrad, *lrem_g;
+    double TU, DZTU, DZTB;
     int izCon, iTCon, iBCon, pad_;
     const double *dxxdx, *d2xxdx2, *DDX;
     const double *dyydy, *d2yydy2, *DDY;
@@ -87,6 +94,10 @@ int parity_fluxes_ext(unsigned sw, const Grid& g, const Consts& c, Fields8 U, Fi
 int parity_rk(int kind, int nf, const Grid& g, Fields8 U, Fields8 Z, Fields8 F, double coef, cudaStream_t st);
 int parity_bcon(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
 int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st);
+// lRem: horizontal means of T per z (in the reference's summation order when
+// `exact`, else by a parallel reduction), then HRAD and the fused form
+// G = HRAD - d2(TTM)/dz2, into buf = [TTM | HRAD | G] (3 x nz doubles).
+int lrem_profiles(const Grid& g, const Consts& c, const double* TT, double* buf, bool exact, cudaStream_t st);
 // CFL partial minima/maxima; out[0..4] = UMACH^2-candidate max, w0..w3 minima.
 int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
                double* out5, cudaStream_t st);

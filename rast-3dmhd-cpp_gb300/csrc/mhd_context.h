@@ -56,6 +56,7 @@ struct mhd_ctx {
     bool plume_set = false;
     double pl_TP = 0.0, pl_TC = 0.0, pl_QFH = 0.0, pl_OCV = 0.0;
     double* d_plume = nullptr;  // plx (nx), ply (ny), plz (nz)
+    double* d_lrem = nullptr;   // lRem: TTM, HRAD, G (3 x nz)
     // host-to-host steps: copy streams and per-slab events (created on first use)
     cudaStream_t s_up = nullptr, s_down = nullptr;
     std::vector<cudaEvent_t> slab_events;

@@ -231,7 +231,13 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 double lapT = acc_d2<!UXY>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
                 lapT = acc_d2<!UXY>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
                 lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
-                ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+                if (c.lrem && !SW::lShr) {
+                    // lRem: conduction of T - TTM(z) plus HRAD (3dmhdsub.h:297-313),
+                    // as lap T + (HRAD - d2 TTM/dz2), the latter precomputed per z
+                    ft = fma(ri * (c.OCV / c.REPR), lapT + c.lrem_g[z], ft);
+                } else {
+                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+                }
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
             if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
@@ -382,7 +388,9 @@ __device__ __forceinline__ void bcon_cell(const Grid& g, const Consts& c, const 
                  c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
         } else if (c.iTCon == 1) {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
-            tt = c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA;
+            tt = c.lrem ? c.C43 * TT[i1] - c.C13 * TT[i2] + c.DZTU : c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA;
+        } else if (c.lrem) {
+            tt = c.TU;
         } else {
             tt = 1.0;
             if (c.iTCon == 4 && x < g.nx / 2) tt = 1.0f - c.TP;
@@ -390,6 +398,8 @@ __device__ __forceinline__ void bcon_cell(const Grid& g, const Consts& c, const 
     } else {
         if (c.izCon == 0) {
             tt = c.TB;
+        } else if (c.lrem) {
+            tt = c.C43 * TT[i1] - c.C13 * TT[i2] + c.DZTB;
         } else {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
             tt = c.C43 * TT[i1] - c.C13 * TT[i2] - c.C23 * DZ * c.THETA / c.RKAPA[z];

@@ -151,12 +151,30 @@ __global__ void k_flux(Grid g, Consts c, Fields8 U, Fields8 F, const double* __r
         } else {
             ft = F.p[F_FT][i];
         }
-        // conduction, 3dmhdsub.h:315-319
         double tmp = c.OCV / c.REPR;
-        ft += ((d2x(TT, i, x, c) * ri) * c.RKAPA[z]) * tmp;
-        ft += ((d2y(TT, i, sy, y, c) * ri) * c.RKAPA[z]) * tmp;
-        ft += ((d2z(TT, i, sz, z, c) * ri) * c.RKAPA[z]) * tmp;
-        ft += ((d1z(TT, i, sz, z, c) * ri) * c.DKAPA[z]) * tmp;
+        if (c.lrem && !SW::lShr) {
+            // lRem: conduction of W = T - TTM(z) plus the mean profile's HRAD,
+            // 3dmhdsub.h:297-313 (W at the stencil points as the reference stores it)
+            const double* M = c.lrem_ttm;
+            const double wc = tt - M[z];
+            const double wxp = TT[i + 1] - M[z], wxm = TT[i - 1] - M[z];
+            const double wyp = TT[i + sy] - M[z], wym = TT[i - sy] - M[z];
+            const double wzp = TT[i + sz] - M[z + 1], wzm = TT[i - sz] - M[z - 1];
+            const double dx = c.dxxdx[x], dy = c.dyydy[y], dz = c.dzzdz[z];
+            const double d2wx = ((wxp - wxm) * c.d2xxdx2[x]) * c.hx + (((wxp - 2 * wc) + wxm) * (dx * dx)) * c.h2x;
+            const double d2wy = ((wyp - wym) * c.d2yydy2[y]) * c.hy + (((wyp - 2 * wc) + wym) * (dy * dy)) * c.h2y;
+            const double d2wz = ((wzp - wzm) * c.d2zzdz2[z]) * c.hz + (((wzp - 2 * wc) + wzm) * (dz * dz)) * c.h2z;
+            ft += (d2wx * ri) * tmp;
+            ft += (d2wy * ri) * tmp;
+            ft += (d2wz * ri) * tmp;
+            ft += (ri * c.lrem_hrad[z]) * tmp;
+        } else {
+            // conduction, 3dmhdsub.h:315-319
+            ft += ((d2x(TT, i, x, c) * ri) * c.RKAPA[z]) * tmp;
+            ft += ((d2y(TT, i, sy, y, c) * ri) * c.RKAPA[z]) * tmp;
+            ft += ((d2z(TT, i, sz, z, c) * ri) * c.RKAPA[z]) * tmp;
+            ft += ((d1z(TT, i, sz, z, c) * ri) * c.DKAPA[z]) * tmp;
+        }
         // internal plume heat sink (iTCon 2), 3dmhdsub.h:443-459
         if (c.pl_mode == 3) ft -= (((c.pl_s * ri) * c.plx[x]) * c.ply[y]) * c.plz[z];
 
@@ -400,7 +418,10 @@ __global__ void k_bcon(Grid g, Consts c, Fields8 U, double timt) {
                 c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
     } else if (c.iTCon == 1) {
         const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[zl];
-        TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] - c.C23 * DZ * c.THETA;
+        if (c.lrem) TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] + c.DZTU;  // 3dmhdsub.h:800-802
+        else TT[i] = c.C43 * TT[i + sz] - c.C13 * TT[i + 2 * sz] - c.C23 * DZ * c.THETA;
+    } else if (c.lrem) {
+        TT[i] = c.TU;  // 3dmhdsub.h:783-784
     } else {
         TT[i] = 1.0f;
         if (c.iTCon == 4 && x < g.nx / 2) TT[i] = 1.0f - c.TP;
@@ -420,6 +441,8 @@ __global__ void k_bcon(Grid g, Consts c, Fields8 U, double timt) {
     RW[i] = 0.0f;
     if (c.izCon == 0) {
         TT[i] = c.TB;
+    } else if (c.lrem) {
+        TT[i] = c.C43 * TT[i - sz] - c.C13 * TT[i - 2 * sz] + c.DZTB;  // 3dmhdsub.h:852-854
     } else {
         const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[zr - 1];
         TT[i] = c.C43 * TT[i - sz] - c.C13 * TT[i - 2 * sz] - c.C23 * DZ * c.THETA / c.RKAPA[zr - 1];
@@ -469,8 +492,11 @@ __global__ void k_comm(int nf, Grid g, Fields8 U) {
 __device__ __forceinline__ double cfl_dd_yz(const Consts& c, int y, int z) {
     return (c.DDZ[z] < c.DDY[y]) ? c.DDZ[z] : c.DDY[y];
 }
+__device__ __forceinline__ double cfl_kappa(const Consts& c, int z) {
+    return c.lrem ? 1.0f + c.RKAPA[z] : c.RKAPA[z];  // 3dmhdsub.h:79-83
+}
 __device__ __forceinline__ double cfl_a1(const Consts& c, double DD, double ro, int z) {
-    return 0.5f * DD * DD * c.REPR * c.CV * ro / c.RKAPA[z];
+    return 0.5f * DD * DD * c.REPR * c.CV * ro / cfl_kappa(c, z);
 }
 __device__ __forceinline__ double cfl_a2(const Consts& c, double DD, double ro) { return 0.375f * DD * DD * c.RE * ro; }
 __device__ __forceinline__ double cfl_a3(const Consts& c, double DD) { return 0.5f * DD * DD * c.RM; }
@@ -589,7 +615,7 @@ __device__ __forceinline__ bool cfl_fast_row(const Grid& g, const Consts& c, int
     const double P1 = 0.5f * DDyz * DDyz * c.REPR * c.CV;  // prefix of cfl_a1
     const double P2 = 0.375f * DDyz * DDyz * c.RE;         // prefix of cfl_a2
     const bool consts_ok = (c.GAMMA >= 0x1p-10 && c.GAMMA <= 0x1p10) && (c.OBETA >= 0.0 && c.OBETA <= 0x1p30);
-    return consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 && c.RKAPA[z] > 0.0;
+    return consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 && cfl_kappa(c, z) > 0.0;
 }
 
 // Seeds of the filter: the smallest a0 estimate and the largest mc estimate
@@ -912,6 +938,55 @@ int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st) {
     return (int)cudaGetLastError();
 }
 
+// horizontal_mean (3dmhdsub.h:698-718) of T on every z plane, one thread per
+// plane summing in the reference's order (y, then x)
+__global__ void k_lrem_ttm_exact(Grid g, const double* TT, double* ttm) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= g.nz) return;
+    double w = 0;
+    for (int y = 1; y < g.ny - 1; y++)
+        for (int x = 1; x < g.nx - 1; x++) w += TT[(long long)z * g.sz + (long long)y * g.sy + x];
+    ttm[z] = w / (float)((g.nx - 2) * (g.ny - 2));
+}
+
+// the same by a block reduction per plane (any summation order)
+__global__ void k_lrem_ttm_fast(Grid g, const double* TT, double* ttm) {
+    __shared__ double s[256];
+    const int z = blockIdx.x;
+    const int n = (g.nx - 2) * (g.ny - 2);
+    double w = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int y = 1 + k / (g.nx - 2), x = 1 + k % (g.nx - 2);
+        w += TT[(long long)z * g.sz + (long long)y * g.sy + x];
+    }
+    s[threadIdx.x] = w;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) ttm[z] = s[0] / (float)n;
+}
+
+// HRAD (3dmhdsub.h:309-312) and G = HRAD - d2(TTM)/dz2 for interior z
+__global__ void k_lrem_hrad(Grid g, Consts c, const double* TTM, double* hrad, double* G) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= g.nz) return;
+    if (z < 1 || z > g.nz - 2) {
+        hrad[z] = 0.0;
+        G[z] = 0.0;
+        return;
+    }
+    double h = (((TTM[z + 1] - 2.0f * TTM[z] + TTM[z - 1])) * c.h2z * c.dzzdz[z] * c.dzzdz[z] +
+                (TTM[z + 1] - TTM[z - 1]) * c.hz * c.d2zzdz2[z]) * c.RKAPA[z];
+    h += (TTM[z + 1] - TTM[z - 1]) * c.hz * c.dzzdz[z] * c.DKAPA[z];
+    hrad[z] = h;
+    const double dz = c.dzzdz[z];
+    const double d2m = ((TTM[z + 1] - TTM[z - 1]) * c.d2zzdz2[z]) * c.hz +
+                       (((TTM[z + 1] - 2 * TTM[z]) + TTM[z - 1]) * (dz * dz)) * c.h2z;
+    G[z] = h - d2m;
+}
+
 int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks, double* out5,
                cudaStream_t st) {
     const int nb = launch_cfl_rows(mag, g, c, U, partials, max_blocks, st);
@@ -923,6 +998,14 @@ int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double
                      double* rec, cudaStream_t st) {
     const int nb = launch_cfl_rows(mag, g, c, U, partials, max_blocks, st);
     k_cfl_record<<<1, 256, 0, st>>>(partials, nb, c.SFF, mag ? 1 : 0, rec);
+    return (int)cudaGetLastError();
+}
+
+int lrem_profiles(const Grid& g, const Consts& c, const double* TT, double* buf, bool exact, cudaStream_t st) {
+    double *ttm = buf, *hrad = buf + g.nz, *G = buf + 2 * g.nz;
+    if (exact) k_lrem_ttm_exact<<<(g.nz + 63) / 64, 64, 0, st>>>(g, TT, ttm);
+    else k_lrem_ttm_fast<<<g.nz, 256, 0, st>>>(g, TT, ttm);
+    k_lrem_hrad<<<(g.nz + 63) / 64, 64, 0, st>>>(g, c, ttm, hrad, G);
     return (int)cudaGetLastError();
 }
 

@@ -69,8 +69,9 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
         b.push_back(nz - 1);
     }
     const int ns = (int)b.size() - 1;
-    if (ns < 3) {
-        // too thin to pipeline: upload, step, download
+    if (ns < 3 || ctx->c.lrem) {
+        // too thin to pipeline (or lRem, whose substages need whole-plane
+        // means first): upload, step, download
         int rc = in ? mhd_upload_state(ctx, in) : MHD_OK;
         if (!rc) rc = mhd_step(ctx, dt, nullptr);
         if (!rc && out) rc = mhd_download_state(ctx, out);

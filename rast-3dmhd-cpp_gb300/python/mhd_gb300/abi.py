@@ -36,7 +36,7 @@ class MhdParams(C.Structure):
                 ("precision", C.c_int), ("path", C.c_int), ("reserved_i", C.c_int * 5)] + \
                [(n, C.c_double) for n in ("RE", "PR", "THETA", "GRAV", "RY", "ANG", "RM", "BETA", "TP", "GAMMA",
                                            "SFF", "TB")] + \
-               [("reserved_d", C.c_double * 4)] + \
+               [(n, C.c_double) for n in ("TU", "DZTU", "DZTB")] + [("reserved_d", C.c_double * 1)] + \
                [(n, _DP) for n in ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ",
                                    "RKAPA", "DKAPA")]
 

@@ -41,6 +41,7 @@ class Case:
     lMag: bool = True
     lRot: bool = False
     lShr: bool = False
+    lRem: bool = False      # Rempel relaxation (3dmhdparam.h:14); needs TU, DZTU, DZTB
     izCon: int = 0          # 0 fixed bottom temperature TB, 1 fixed flux (3dmhdsub.h:842-864)
     iTCon: int = 0          # 0/1/4 upper temperature condition (3dmhdsub.h:750-810)
     iBCon: int = 0          # 0: Bz = 0 on both walls (3dmhdsub.h:811-817,865-871)
@@ -62,6 +63,10 @@ class Case:
     HH: float = 0.0
     TC: float = 0.0
     QFH: float = 0.0
+    # lRem wall values of the static model (Static(), 3dmhdphsic.h:592-594)
+    TU: float = 1.0
+    DZTU: float = 0.0
+    DZTB: float = 0.0
     xMax: float = 6.0
     yMax: float = 6.0
     zMax: float = 2.0
@@ -310,6 +315,18 @@ def plume_cases() -> dict[str, Case]:
         "plume_top1": Case(name="plume_top1", lMag=False, iTCon=1, izCon=1, TP=0.3, **base),
         "plume_src2": Case(name="plume_src2", lRot=True, iTCon=2, TP=2.0, TC=1e-4, QFH=2e-4,
                            **dict(base, HH=1.0, ZP=1.0)),
+    }
+
+
+def lrem_cases() -> dict[str, Case]:
+    """lRem (Rempel relaxation) cases on one y rank (the reference's
+    horizontal_mean sums over every rank when nPEy > 1, 3dmhdsub.h:714-717):
+    a fixed top temperature TU with iTCon 0 and the fixed-gradient walls
+    (DZTU, DZTB) with iTCon 1, izCon 1."""
+    base = dict(nPx=12, nPy=8, nPz=8, nPEy=1, nPEz=2, seed=7, noise=1e-2, bz0=1e-2, dt=2e-4, lRem=True)
+    return {
+        "lrem_fixedT": Case(name="lrem_fixedT", iTCon=0, izCon=0, TU=1.05, **base),
+        "lrem_flux": Case(name="lrem_flux", lMag=False, lRot=True, iTCon=1, izCon=1, DZTU=-0.03, DZTB=0.02, **base),
     }
 
 

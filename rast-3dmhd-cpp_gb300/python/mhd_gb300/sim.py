@@ -22,7 +22,8 @@ def params_for(case: Case, path: str = "fused", precision: str = "fp64") -> tupl
     p = abi.MhdParams()
     p.nPx, p.nPy, p.nPz = case.nPx, case.nPy, case.nPz
     p.switches = (abi.SW_LROT if case.lRot else 0) | (abi.SW_LMAG if case.lMag else 0) | \
-                 (abi.SW_LSHR if case.lShr else 0)
+                 (abi.SW_LSHR if case.lShr else 0) | (abi.SW_LREM if case.lRem else 0)
+    p.TU, p.DZTU, p.DZTB = float(case.TU), float(case.DZTU), float(case.DZTB)
     p.ixCon = p.iyCon = 0
     p.izCon, p.iTCon, p.iBCon = case.izCon, case.iTCon, case.iBCon
     p.precision = abi.PREC_FP64 if precision == "fp64" else abi.PREC_FP32

@@ -20,7 +20,13 @@ def pytest_configure(config):
 
 def golden_case_names():
     """The small switch-coverage cases (GPU tests replay their fixtures)."""
-    return sorted(k for k in json.loads((GOLDEN / "cases.json").read_text()) if not k.startswith("plume_"))
+    return sorted(k for k in json.loads((GOLDEN / "cases.json").read_text())
+                  if not k.startswith("plume_") and not k.startswith("lrem_"))
+
+
+def lrem_case_names():
+    """The lRem cases (Rempel relaxation, one y rank)."""
+    return sorted(k for k in json.loads((GOLDEN / "cases.json").read_text()) if k.startswith("lrem_"))
 
 
 def plume_case_names():

@@ -5,8 +5,9 @@ override with MHD_REFERENCE_DIR):
 
     python tests/golden/make_golden.py
 
-For every small switch-coverage case (mhd_gb300.case.small_cases, and the
-plume cases of mhd_gb300.case.plume_cases) it builds
+For every small switch-coverage case (mhd_gb300.case.small_cases, the
+plume cases of mhd_gb300.case.plume_cases and the lRem cases of
+mhd_gb300.case.lrem_cases) it builds
 the reference with oracle/refcase.py (2 x 2 forked MPI ranks), feeds it the
 seeded initial state and stores, as <case>.npz:
   in_*      the input state and metric arrays (so the fixture does not depend
@@ -34,10 +35,10 @@ sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
 
 import refcase  # noqa: E402
 from mhd_gb300.case import (FLUX_FIELDS, STATE_FIELDS, config0, config1, initial_state, metrics,  # noqa: E402
-                            plume_cases, small_cases)
+                            lrem_cases, plume_cases, small_cases)
 
 METRIC_NAMES = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
-CFL_CASES = ("mhd_fixedT", "hydro_default_bc")
+CFL_CASES = ("mhd_fixedT", "hydro_default_bc", "lrem_fixedT", "lrem_flux")
 
 
 def sha(a: np.ndarray) -> str:
@@ -48,7 +49,7 @@ def main() -> None:
     if not refcase.reference_available():
         raise SystemExit(f"reference sources not found under {refcase.REF_DIR}")
     manifest = {}
-    for name, case in list(small_cases().items()) + list(plume_cases().items()):
+    for name, case in list(small_cases().items()) + list(plume_cases().items()) + list(lrem_cases().items()):
         st = initial_state(case)
         m = metrics(case)
         out = {}

@@ -62,11 +62,15 @@ def test_invalid_configs_rejected_without_gpu(lib, change, status):
 
 
 def test_lrem_and_nonperiodic_rejected(lib):
-    case = small_cases()["mhd_fixedT"]
+    """lRem with lShr (the reference then reads unfilled arrays) and lRem in
+    FP32 storage are rejected, as are non-periodic horizontal walls."""
+    case = small_cases()["mhd_rot_shr"].replace(lRem=True)
     p, keep = params_for(case)
-    p.switches |= abi.SW_LREM
     ctx = C.c_void_p()
     assert lib.mhd_create(C.byref(p), None, C.byref(ctx)) == -2
+    p, keep = params_for(small_cases()["mhd_fixedT"].replace(lRem=True), precision="fp32")
+    assert lib.mhd_create(C.byref(p), None, C.byref(ctx)) == -2
+    case = small_cases()["mhd_fixedT"]
     p, keep = params_for(case)
     p.ixCon = 1
     assert lib.mhd_create(C.byref(p), None, C.byref(ctx)) == -2

@@ -108,6 +108,38 @@ def test_scheduler_admits_under_budget_and_completes_every_request(fake_backend)
     assert st["tts_p99_s"] >= st["tts_p50_s"] > 0
 
 
+def test_srpt_admits_least_work_first_and_caps_resident_cells(fake_backend):
+    """With "srpt" the waiting request with the least work is admitted first
+    and resident work stays near target_cells; every request still runs
+    exactly its step count."""
+    reqs = poisson_requests(30, rate=1e6, seed=3, grid_min=(16, 16, 8), grid_max=(64, 64, 32), steps=(3, 40))
+    for r in reqs:
+        r.arrival = 0.0
+    target = 3 * max(r.case.cells for r in reqs)
+    srv = Server(1 << 40, quantum=5, keep_results=True, policy="srpt", target_cells=target)
+    order = []
+    orig = srv._admit
+
+    def spy(req, now):
+        ok = orig(req, now)
+        if ok:
+            order.append(req)
+            assert srv.resident_cells <= target + req.case.cells
+        return ok
+    srv._admit = spy
+    st = srv.run(reqs, realtime=False)
+    assert st["policy"] == "srpt" and FakeSim.live == 0 and srv.resident_cells == 0
+    assert all(r.result["steps"] == r.steps for r in reqs)
+    # all arrived at once: the first admissions are the least-work requests
+    work = sorted(r.case.cells * r.steps for r in reqs)
+    first = [r.case.cells * r.steps for r in order[:3]]
+    assert first == work[:3]
+    fifo = Server(1 << 40, quantum=5, policy="fifo").run(
+        poisson_requests(30, rate=1e6, seed=3, grid_min=(16, 16, 8), grid_max=(64, 64, 32), steps=(3, 40)),
+        realtime=False)
+    assert fifo["policy"] == "fifo" and fifo["max_resident"] >= st["max_resident"]
+
+
 def test_scheduler_rejects_a_request_larger_than_the_budget(fake_backend):
     big = Request(rid=0, case=poisson_requests(1, 1.0, seed=2)[0].case, steps=3)
     with pytest.raises(RuntimeError):

@@ -6,7 +6,7 @@ import json
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_case_names, load_golden, plume_case_names
+from conftest import GOLDEN, golden_case_names, load_golden, lrem_case_names, plume_case_names
 from mhd_gb300.case import FLUX_FIELDS, STATE_FIELDS, config0, initial_state
 
 import oracle
@@ -24,7 +24,7 @@ def oracle_from_fixture(case, g):
     return sim
 
 
-@pytest.mark.parametrize("name", golden_case_names() + plume_case_names())
+@pytest.mark.parametrize("name", golden_case_names() + plume_case_names() + lrem_case_names())
 def test_fluxes_bit_exact(name):
     case, g = load_golden(name)
     sim = oracle_from_fixture(case, g)
@@ -35,7 +35,7 @@ def test_fluxes_bit_exact(name):
         assert np.array_equal(got, g["flux_" + k]), k
 
 
-@pytest.mark.parametrize("name", golden_case_names() + plume_case_names())
+@pytest.mark.parametrize("name", golden_case_names() + plume_case_names() + lrem_case_names())
 def test_three_steps_bit_exact(name):
     case, g = load_golden(name)
     sim = oracle_from_fixture(case, g)
@@ -44,7 +44,7 @@ def test_three_steps_bit_exact(name):
         assert np.array_equal(sim.arr[k], g["steps3_" + k]), k
 
 
-@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc"])
+@pytest.mark.parametrize("name", ["mhd_fixedT", "hydro_default_bc", "lrem_fixedT", "lrem_flux"])
 def test_cfl_steps_bit_exact(name):
     case, g = load_golden(name)
     sim = oracle_from_fixture(case, g)
