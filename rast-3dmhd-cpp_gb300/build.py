@@ -27,6 +27,7 @@ UNITS = [
     ("mhd_abi.cu", "mhd_abi", []),
     ("mhd_parity.cu", "mhd_parity", ["-fmad=false"]),
     ("mhd_fused.cu", "mhd_fused", []),
+    ("mhd_fused.cu", "mhd_fused_xp", ["-DMHD_FUSED_XP=1"]),
     ("mhd_fused_batch.cu", "mhd_fused_batch_uxy", ["-DMHD_BATCH_UXY=1"]),
     ("mhd_fused_batch.cu", "mhd_fused_batch_gen", ["-DMHD_BATCH_UXY=0"]),
     ("mhd_diag.cu", "mhd_diag", []),

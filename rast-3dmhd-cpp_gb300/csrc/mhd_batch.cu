@@ -376,9 +376,10 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
             fprintf(stderr, "mhd_batch_create: lRem instances step alone (per-substage plane means)\n");
             return MHD_ERR_UNSUPPORTED;
         }
-        if (c->c.pl_mode != 0 && (!c->plume_set || ctxops::plume_time_dependent(c))) {
+        if (c->c.pl_mode == 3 || (c->c.pl_mode != 0 && (!c->plume_set || ctxops::plume_time_dependent(c)))) {
             delete b;
-            fprintf(stderr, "mhd_batch_create: plume terms must be set and time-independent (TC = 0) in a batch\n");
+            fprintf(stderr, "mhd_batch_create: batched instances may carry only a time-independent top-wall plume "
+                            "(TC = 0); the iTCon 2 heat sink steps alone\n");
             return MHD_ERR_UNSUPPORTED;
         }
         if (i > 0 && (c->sw != b->sw || c->fp32 != b->fp32)) {

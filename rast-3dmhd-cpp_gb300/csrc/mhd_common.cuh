@@ -135,6 +135,8 @@ constexpr int kDtRecord = 8;
 int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
                      double* rec, cudaStream_t st);
 int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st);
+// the instantiation with the optional temperature terms (fused_substage calls it)
+int fused_substage_xp(unsigned sw, const FusedArgs& a, cudaStream_t st);
 // Ragged batches: persistent CTAs take (instance, tile x, tile y) items from a
 // counter that must be zero at launch.  Tile shapes: 0 = 32x4, 1 = 32x8, 2 = 16x8.
 constexpr int kBatchTiles = 3;

@@ -99,8 +99,9 @@ __device__ __forceinline__ void store32_with_images(float* F, const Grid& g, int
     }
 }
 
-// One tile (bx, by) of one instance, interior z planes [zb, ze).
-template <class SW>
+// One tile (bx, by) of one instance, interior z planes [zb, ze).  EXTRA: the
+// instantiation with the iTCon 2 plume heat sink.
+template <class SW, bool EXTRA = false>
 __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, int by, int zb, int ze,
                                                 unsigned char* ring) {
     constexpr int NQ = nqf<SW>();
@@ -204,8 +205,10 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 ft = fmaf(ri * tmpc, fmaf(a.zf[5 * nzz + z], lapT, a.zf[6 * nzz + z] * Tz), ft);
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
-            if (c.pl_mode == 3)
-                ft = fmaf(-(float)c.pl_s * ri, (float)(c.plx[x] * c.ply[y] * c.plz[z]), ft);
+            if constexpr (EXTRA) {
+                if (c.pl_mode == 3)
+                    ft = fmaf(-(float)c.pl_s * ri, (float)(c.plx[x] * c.ply[y] * c.plz[z]), ft);
+            }
 
             // ---- viscous Laplacians and cross terms
             fu = fmaf(ore43, D2x(F_U), fmaf(ore, D2y(F_U) + D2z(F_U), fu));
@@ -322,13 +325,13 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
 }
 
 // one instance: grid (x tiles, y tiles, z chunks)
-template <class SW>
+template <class SW, bool EXTRA>
 __global__ void __launch_bounds__(kThreads, 3) k_substage32(Fused32Args a) {
     extern __shared__ __align__(16) unsigned char ring[];
     const int nPz = a.g.nz - 2;
     const int zb = 1 + (int)((long long)nPz * blockIdx.z / gridDim.z);
     const int ze = 1 + (int)((long long)nPz * (blockIdx.z + 1) / gridDim.z);
-    substage32_tile<SW>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
+    substage32_tile<SW, EXTRA>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
 }
 
 // ragged batch: persistent CTAs take (instance, tile x, tile y, z range) items
@@ -480,22 +483,28 @@ int chunks32(long long tiles, int slots, int nPz) {
     return best;
 }
 
-template <class SW>
-void launch32(const Fused32Args& a, cudaStream_t st, int* rc) {
+template <class SW, bool EXTRA>
+void launch32_t(const Fused32Args& a, cudaStream_t st, int* rc) {
     const size_t smem = 3 * plane_bytes<SW>();
     static int slots = 0;
     if (!slots) {
-        cudaFuncSetAttribute(k_substage32<SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_substage32<SW, EXTRA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int dev = 0, sms = 0, per_sm = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substage32<SW>, kThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substage32<SW, EXTRA>, kThreads, smem);
         slots = sms * (per_sm > 0 ? per_sm : 1);
     }
     const int nbx = (a.g.nx - 2 + kTX - 1) / kTX, nby = (a.g.ny - 2 + kTY - 1) / kTY;
     const int chunks = chunks32((long long)nbx * nby, slots, a.g.nz - 2);
-    k_substage32<SW><<<dim3(nbx, nby, chunks), kThreads, smem, st>>>(a);
+    k_substage32<SW, EXTRA><<<dim3(nbx, nby, chunks), kThreads, smem, st>>>(a);
     *rc = (int)cudaGetLastError();
+}
+
+template <class SW>
+void launch32(const Fused32Args& a, cudaStream_t st, int* rc) {
+    if (a.c.pl_mode == 3) launch32_t<SW, true>(a, st, rc);
+    else launch32_t<SW, false>(a, st, rc);
 }
 
 template <class SW>

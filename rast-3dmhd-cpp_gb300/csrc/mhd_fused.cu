@@ -17,6 +17,13 @@ using namespace fused;
 #ifndef MHD_FUSED_TILE_Y
 #define MHD_FUSED_TILE_Y 4
 #endif
+// This file is compiled twice: MHD_FUSED_XP=0 gives the kernels without the
+// optional temperature terms (and the dispatcher and the wall kernels),
+// MHD_FUSED_XP=1 the ones with the iTCon 2 heat sink and lRem.
+#ifndef MHD_FUSED_XP
+#define MHD_FUSED_XP 0
+#endif
+constexpr bool kExtra = MHD_FUSED_XP != 0;
 using DefaultTile = Tile<32, MHD_FUSED_TILE_Y>;
 constexpr int kMinBlocks = DefaultTile::kThreads >= 256 ? 2 : 3;
 
@@ -27,7 +34,7 @@ __global__ void __launch_bounds__(DefaultTile::kThreads, kMinBlocks) k_substage(
     const int nz = (a.zhi > 0 ? a.zhi : a.g.nz - 1) - lo;
     const int zb = lo + (int)((long long)nz * blockIdx.z / gridDim.z);
     const int ze = lo + (int)((long long)nz * (blockIdx.z + 1) / gridDim.z);
-    substage_tile<SW, DefaultTile, UXY>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
+    substage_tile<SW, DefaultTile, UXY, kExtra>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
 }
 
 template <class SW>
@@ -89,7 +96,15 @@ void launch_bcon_ghost(const Grid& g, const Consts& c, Fields8 U, double timt, i
 
 }  // namespace
 
+#if MHD_FUSED_XP
+int fused_substage_xp(unsigned sw, const FusedArgs& a, cudaStream_t st) {
+    int rc = 0;
+    MHD_DISPATCH_SW(sw, launch_substage, a, st, &rc);
+    return rc;
+}
+#else
 int fused_substage(unsigned sw, const FusedArgs& a, cudaStream_t st) {
+    if (a.c.pl_mode == 3 || a.c.lrem) return fused_substage_xp(sw, a, st);
     int rc = 0;
     MHD_DISPATCH_SW(sw, launch_substage, a, st, &rc);
     return rc;
@@ -104,5 +119,6 @@ int fused_bcon_wall(unsigned sw, const Grid& g, const Consts& c, Fields8 U, doub
     MHD_DISPATCH_SW(sw, launch_bcon_ghost, g, c, U, timt, wall, st);
     return (int)cudaGetLastError();
 }
+#endif
 
 }  // namespace mhd

@@ -128,7 +128,9 @@ __device__ __forceinline__ double acc_d2(double acc, double p, double m, double 
 }
 
 // One tile (bx, by) of one instance, z planes [zb, ze) of the interior.
-template <class SW, class T, bool UXY>
+// EXTRA: the instantiation with the optional temperature terms (the iTCon 2
+// plume heat sink, lRem); the others carry no code for them.
+template <class SW, class T, bool UXY, bool EXTRA = false>
 __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by, int zb, int ze, double* ring) {
     constexpr int NQ = nq<SW>();
     constexpr int kTX = T::kTX, kPX = T::kPX, kPlane = T::kPlane, kTY = T::kTY;
@@ -231,7 +233,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 double lapT = acc_d2<!UXY>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
                 lapT = acc_d2<!UXY>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
                 lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
-                if (c.lrem && !SW::lShr) {
+                if (EXTRA && c.lrem && !SW::lShr) {
                     // lRem: conduction of T - TTM(z) plus HRAD (3dmhdsub.h:297-313),
                     // as lap T + (HRAD - d2 TTM/dz2), the latter precomputed per z
                     ft = fma(ri * (c.OCV / c.REPR), lapT + c.lrem_g[z], ft);
@@ -240,7 +242,9 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 }
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
-            if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
+            if constexpr (EXTRA) {
+                if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
+            }
 
             // ---- viscous Laplacians (3dmhdsub.h:462-472)
             fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
