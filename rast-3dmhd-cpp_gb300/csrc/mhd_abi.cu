@@ -239,7 +239,18 @@ int set_profile(mhd_ctx* ctx, int field, const double* host) {
             for (int x = 1; x < nx - 1; x++) s += host[((size_t)z * ny + y) * nx + x];
         bg[z] = s / ((double)(nx - 2) * (ny - 2));
     }
-    if (field == MHD_TT) {
+    return ctxops::profiles_from_means(ctx);
+}
+
+}  // namespace
+
+namespace mhd::ctxops {
+// With rho0 and T0 in h_bg: T0's premultiplied z derivatives, the float
+// coefficient table, and both uploaded.
+int profiles_from_means(mhd_ctx* ctx) {
+    const int nz = ctx->g.nz;
+    const double* bg = ctx->h_bg.data() + nz;
+    {
         double* d1 = ctx->h_bg.data() + 2 * nz;
         double* d2 = ctx->h_bg.data() + 3 * nz;
         const double *cz1 = ctx->h_cz.data(), *cz2a = cz1 + nz, *cz2b = cz1 + 2 * nz;
@@ -259,6 +270,9 @@ int set_profile(mhd_ctx* ctx, int field, const double* host) {
     CK(cudaMemcpy(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz, cudaMemcpyHostToDevice));
     return MHD_OK;
 }
+}  // namespace mhd::ctxops
+
+namespace {
 
 int upload32(mhd_ctx* ctx, int field, const double* host) {
     if (field == MHD_RO || field == MHD_TT) {

@@ -78,6 +78,9 @@ void advance_time(mhd_ctx* c, double dt);
 int plume_update(mhd_ctx* c, double timt);
 // whether the plume terms depend on the simulation time (TC != 0)
 bool plume_time_dependent(const mhd_ctx* c);
+// FP32 contexts: with rho0(z), T0(z) in h_bg, derive T0's z derivatives and
+// the float coefficient table and upload the profiles
+int profiles_from_means(mhd_ctx* c);
 // FusedArgs of substage s (0..2) of the fused FP64 step reading state buffer
 // U[in] and writing U[1-in]
 FusedArgs fused_args(const mhd_ctx* c, int s, double dt, int in);

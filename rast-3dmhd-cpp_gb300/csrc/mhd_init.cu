@@ -69,16 +69,44 @@ __global__ void k_init(Grid g, Fields8 U, const double* zc, double theta, double
     }
 }
 
+// horizontal mean of F over the interior of every z plane (one block per plane)
+__global__ void k_plane_mean(Grid g, const double* F, double* out) {
+    __shared__ double s[256];
+    const int z = blockIdx.x, nx = g.nx - 2, n = nx * (g.ny - 2);
+    double w = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        w += F[(long long)z * g.sz + (long long)(1 + k / nx) * g.sy + 1 + k % nx];
+    s[threadIdx.x] = w;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[z] = s[0] / ((double)nx * (g.ny - 2));
+}
+
+// FP32 storage: deviation of every FP64 field from its profile (rho0, T0 for RO, TT)
+__global__ void k_to_f32(Grid g, int nf, Fields8 Z, Fields8f U, const double* rho0, const double* t0) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(i / g.sz);
+        for (int f = 0; f < nf; f++) {
+            const double prof = (f == S_RO) ? rho0[z] : (f == S_TT) ? t0[z] : 0.0;
+            U.p[f][i] = (float)(Z.p[f][i] - prof);
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" int mhd_init_polytrope(mhd_ctx* ctx, const double* zcoord, double noise, unsigned long long seed,
                                   double bz0) {
     if (!ctx || !zcoord) return MHD_ERR_INVALID;
-    if (ctx->fp32) return ctxops::fail(ctx, MHD_ERR_UNSUPPORTED, "device initialisation writes FP64 contexts");
     const int nz = ctx->g.nz;
     double* dz = nullptr;
-    // the z coordinates go into the context's reduction scratch (nz doubles fit: it holds 8 x 1216)
-    if ((size_t)nz > (size_t)8 * ctx->red_blocks) return ctxops::fail(ctx, MHD_ERR_INVALID, "nz too large");
+    // the z coordinates (and, for FP32 contexts, the two plane-mean profiles)
+    // go into the context's reduction scratch (it holds 8 x 1216 doubles)
+    if ((size_t)3 * nz > (size_t)8 * ctx->red_blocks) return ctxops::fail(ctx, MHD_ERR_INVALID, "nz too large");
     dz = ctx->red;
     cudaError_t e = cudaMemcpyAsync(dz, zcoord, sizeof(double) * nz, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return ctxops::fail(ctx, MHD_ERR_CUDA, cudaGetErrorString(e));
@@ -86,11 +114,29 @@ extern "C" int mhd_init_polytrope(mhd_ctx* ctx, const double* zcoord, double noi
     const long long n = (long long)ctx->ncell;
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 32) blocks = 152 * 32;
-    k_init<<<(int)blocks, 256, 0, ctx->stream>>>(ctx->g, ctxops::fields_of(ctx, ctx->U[ctx->cur]), dz, theta, m,
+    // FP32 contexts: the FP64 state goes into the RK register Z (which carries
+    // the state between their steps), then into the FP32 deviation fields
+    double* target = ctx->fp32 ? ctx->Zb : ctx->U[ctx->cur];
+    k_init<<<(int)blocks, 256, 0, ctx->stream>>>(ctx->g, ctxops::fields_of(ctx, target), dz, theta, m,
                                                  noise, seed, bz0, (ctx->sw & kSwMag) ? 1 : 0,
                                                  (ctx->sw & kSwShr) ? 1 : 0);
     e = cudaGetLastError();
     if (e != cudaSuccess) return ctxops::fail(ctx, MHD_ERR_CUDA, cudaGetErrorString(e));
+    if (ctx->fp32) {
+        const Fields8 Z = ctxops::fields_of(ctx, ctx->Zb);
+        double* means = ctx->red + nz;  // rho0, T0
+        k_plane_mean<<<nz, 256, 0, ctx->stream>>>(ctx->g, Z.p[S_RO], means);
+        k_plane_mean<<<nz, 256, 0, ctx->stream>>>(ctx->g, Z.p[S_TT], means + nz);
+        e = cudaMemcpyAsync(ctx->h_bg.data(), means, sizeof(double) * 2 * nz, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctxops::fail(ctx, MHD_ERR_CUDA, cudaGetErrorString(e));
+        const int rc = ctxops::profiles_from_means(ctx);
+        if (rc) return rc;
+        k_to_f32<<<(int)blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->nf, Z, ctxops::fields32_of(ctx, ctx->U32[ctx->cur]),
+                                                      ctx->d_bg, ctx->d_bg + nz);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return ctxops::fail(ctx, MHD_ERR_CUDA, cudaGetErrorString(e));
+    }
     ctx->ghosts_synced = false;
     e = cudaStreamSynchronize(ctx->stream);  // the host z array may go away after return
     return e == cudaSuccess ? MHD_OK : ctxops::fail(ctx, MHD_ERR_CUDA, cudaGetErrorString(e));

@@ -55,18 +55,20 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
     if (ctx->fp32 || ctx->prm.path != MHD_PATH_FUSED)
         return ctxops::fail(ctx, MHD_ERR_UNSUPPORTED, "host-to-host steps run on the fused FP64 path");
     const int nPz = ctx->g.nz - 2, nz = ctx->g.nz;
-    // Interior slab bounds: the first two and the last slab are thin (the
-    // compute waits for two slabs' upload before it starts, and the last
-    // slab's download follows the last kernel), the others about 32 planes;
-    // every slab has at least 4 planes (the wall stencils reach 3 planes in).
+    // Interior slab heights grow geometrically from the bottom wall, 4, 4, 8,
+    // 16, then about 32 planes, and shrink again, 16, 8, 4, at the top: the
+    // compute waits for the first two slabs' upload, each later upload must
+    // fit under the compute of the slabs before it (a plane uploads in about
+    // 0.7x the time its three substages take at 512 x 512), and the last
+    // download follows the last kernel.  Every slab has at least 4 planes (the
+    // wall stencils reach 3 planes in).
     std::vector<int> b{1};
-    if (nPz >= 96) {
-        const int edge = 8;
-        b.push_back(1 + edge);
-        b.push_back(1 + 2 * edge);
-        const int mid = nPz - 3 * edge, nm = std::max(1, (mid + 16) / 32);
-        for (int j = 1; j <= nm; j++) b.push_back(1 + 2 * edge + (int)((long long)mid * j / nm));
-        b.push_back(nz - 1);
+    const int head[4] = {4, 4, 8, 16}, tail[3] = {16, 8, 4};
+    if (nPz >= 92) {
+        for (int h : head) b.push_back(b.back() + h);
+        const int mid = nPz - 32 - 28, nm = std::max(1, (mid + 16) / 32), m0 = b.back();
+        for (int j = 1; j <= nm; j++) b.push_back(m0 + (int)((long long)mid * j / nm));
+        for (int h : tail) b.push_back(b.back() + h);
     }
     const int ns = (int)b.size() - 1;
     if (ns < 3 || ctx->c.lrem) {

@@ -31,7 +31,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .case import Case, STATE_FIELDS, device_initial_state, initial_state
+from .case import Case, STATE_FIELDS, initial_state
 from .sim import Batch, Simulation
 
 
@@ -82,12 +82,12 @@ def poisson_requests(n: int, rate: float, seed: int = 0, grid_min=(32, 32, 32), 
 
 
 def init_state(sim, case: Case, precision: str, device_init: bool) -> None:
-    """Initial state of a request: generated on the GPU for FP64 contexts
-    (the host mirror of the same generator for FP32 ones), or numpy's."""
-    if device_init and precision == "fp64":
+    """Initial state of a request: generated on the GPU (both precisions), or
+    numpy's on the host and uploaded."""
+    if device_init:
         sim.init_on_device()
     else:
-        sim.upload_state(device_initial_state(case) if device_init else initial_state(case))
+        sim.upload_state(initial_state(case))
     sim.communicate()
 
 
@@ -185,25 +185,35 @@ class Server:
                 self.batch_rebuilds += 1
 
     # -- one scheduling quantum --------------------------------------------
-    def _advance(self) -> int:
-        """Queue up to `quantum` steps for every resident simulation; returns
-        how many steps were queued per simulation."""
-        if not self.resident:
-            return 0
-        q = min(self.quantum, min(r.remaining for r in self.resident.values()))
-        for key, b in self.batches.items():
+    def _launch(self) -> tuple[int, list]:
+        """Queue up to `quantum` steps for every simulation in a batch (no
+        wait); returns the steps queued and the requests that take them."""
+        members = [rid for rids in self.batch_members.values() for rid in rids]
+        if not members:
+            return 0, []
+        q = min(self.quantum, min(self.resident[rid].remaining for rid in members))
+        for b in self.batches.values():
             b.steps(q)
-        for r in self.resident.values():
-            r.remaining -= q
-            self.cell_steps += r.req.case.cells * q
+        return q, members
+
+    def _complete(self, q: int, members: list) -> None:
+        """Wait for the queued quantum and account its steps."""
         for b in self.batches.values():
             b.sync()
-        return q
+        for rid in members:
+            r = self.resident[rid]
+            r.remaining -= q
+            self.cell_steps += r.req.case.cells * q
 
     def run(self, requests: list, realtime: bool = True, virtual_step_s: float = 1e-3) -> dict:
         """Serve `requests`.  realtime=False replaces the wall clock by a
         virtual one that advances virtual_step_s per queued step, so a run's
-        admissions are reproducible."""
+        admissions are reproducible.
+
+        Each round queues one quantum for the batched simulations, then
+        admits waiting requests while the GPU works on it (creating a context
+        and its initial state is host work), waits, retires the finished
+        simulations and rebuilds the batches whose membership changed."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         future = deque(reqs)
         waiting: deque = deque()
@@ -216,6 +226,7 @@ class Server:
                 waiting.append(future.popleft())
             if self.policy == "srpt" and len(waiting) > 1:
                 waiting = deque(sorted(waiting, key=lambda r: (r.case.cells * r.steps, r.arrival)))
+            q, members = self._launch()
             changed = False
             while waiting and self._admit(waiting[0], now):
                 waiting.popleft()
@@ -230,16 +241,15 @@ class Server:
                     else:
                         virtual = nxt
                 continue
-            if changed:
-                self._sync_batches()
-            q = self._advance()
-            if not realtime:
-                virtual += q * virtual_step_s
+            if members:
+                self._complete(q, members)
+                if not realtime:
+                    virtual += q * virtual_step_s
             now = clock() if realtime else virtual
             done = [r for r in self.resident.values() if r.remaining <= 0]
             for r in done:
                 self._finish(r, now)
-            if done:
+            if changed or done:
                 self._sync_batches()
         wall = (clock() if realtime else virtual)
         for b in self.batches.values():

@@ -116,3 +116,22 @@ def test_integer_pipe_conversions_match_hardware():
     n = C.c_longlong(-1)
     abi.check(L.mhd_selftest_convert(1 << 24, 20261203, C.byref(n)))
     assert n.value == 0
+
+
+def test_device_initial_state_fp32():
+    """FP32-storage contexts generate their initial state on the device too:
+    the FP64 state in the RK register, plane-mean profiles, FP32 deviations;
+    it matches the host mirror of the generator to the FP32 rounding."""
+    from mhd_gb300.case import device_initial_state
+    case = small_cases()["mhd_rot_shr"].replace(nPx=24, nPy=10, nPz=8, seed=4321)
+    sim = Simulation(case, precision="fp32")
+    sim.init_on_device()
+    got = sim.download_state()
+    want = device_initial_state(case)
+    for k in STATE_FIELDS:
+        scale = max(np.abs(want[k]).max(), 1e-300)
+        assert np.abs(got[k] - want[k]).max() / scale <= 1e-6, k
+    sim.communicate()
+    sim.step(case.dt)
+    assert sim.diagnostics()["nit"] == 1
+    sim.close()

@@ -81,7 +81,6 @@ def fake_backend(monkeypatch):
     monkeypatch.setattr(serve, "Simulation", FakeSim)
     monkeypatch.setattr(serve, "Batch", FakeBatch)
     monkeypatch.setattr(serve, "initial_state", lambda case: {})
-    monkeypatch.setattr(serve, "device_initial_state", lambda case: {})
     FakeSim.live = 0
     yield
 
