@@ -396,8 +396,14 @@ def run_precision(args, dist: Dist) -> None:
         sub_ms, launches = sim.profile_read()
         sim.profile(False)
         d1 = sim.diagnostics(check=False)
-        res[prec] = {"state": sim.download_state(), "ms": ms, "sub_ms": sub_ms, "launches": launches,
-                     "d0": d0, "d1": d1}
+        state = sim.download_state()
+        # the reference's run mode on the same context: 100 steps with a CFL dt each,
+        # reduced on the device into the record the substages read
+        sim.timer_start()
+        sim.steps_cfl(100)
+        ms_cfl = sim.timer_stop()
+        res[prec] = {"state": state, "ms": ms, "sub_ms": sub_ms, "launches": launches,
+                     "d0": d0, "d1": d1, "ms_cfl": ms_cfl}
         sim.close()
     errs = {}
     for k in STATE_FIELDS:
@@ -420,7 +426,10 @@ def run_precision(args, dist: Dist) -> None:
                      "substage_hbm_frac": case.cells * bytes_cs / 3 / avg / 1e9 / hbm,
                      "drift": {k: r["d1"][k] / r["d0"][k] - 1.0 if r["d0"][k] else None
                                for k in ("total_mass", "total_energy")},
-                     "max_divb": [r["d0"]["max_divb"], r["d1"]["max_divb"]]}
+                     "max_divb": [r["d0"]["max_divb"], r["d1"]["max_divb"]],
+                     "adaptive_cfl": {"value": case.cells * 100 / (r["ms_cfl"] / 1e3),
+                                      "ms_per_step": r["ms_cfl"] / 100,
+                                      "cost_vs_fixed_dt": (r["ms_cfl"] / 100) / (r["ms"] / nsteps) - 1.0}}
     out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
     out["errors_fp32_vs_fp64"] = errs
     if dist.rank == 0:

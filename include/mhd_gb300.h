@@ -230,10 +230,11 @@ int mhd_step(mhd_ctx* ctx, double dt, mhd_diag* out);
 int mhd_steps(mhd_ctx* ctx, int n, double dt);
 /* n steps of the reference's run mode, each with its CFL dt (step(),
  * 3dmhdsub.h:36-106, called from the loop of 3dmhd.cpp:271-331).  On the
- * fused FP64 path the dt is reduced into a device-resident record that the
- * substage kernels read, so the n steps are queued without host round trips
- * and the call blocks once, at the end (the FP32-storage and parity paths
- * read dt back each step).  dt agrees bit for bit with mhd_cfl_dt.  When a
+ * fused paths (FP64 and FP32 storage) the dt is reduced into a
+ * device-resident record that the substage kernels read, so the n steps are
+ * queued without host round trips and the call blocks once, at the end (the
+ * unfused path, and a plume whose strength depends on TIMT, read dt back
+ * each step).  dt agrees bit for bit with mhd_cfl_dt.  When a
  * step's dt falls below 1e-8 (the halt of 3dmhd.cpp:292) the state stays as
  * it was before that step and the call returns MHD_ERR_DT_TOO_SMALL
  * (MHD_ERR_NUMERIC for a non-finite dt).  `out` (may be NULL) receives the

@@ -319,7 +319,8 @@ int sync_zghosts32(mhd_ctx* ctx) {
     return MHD_OK;
 }
 
-int fused32_step(mhd_ctx* ctx, double dt) {
+// One FP32-storage step; dtp as for fused_step.
+int fused32_step(mhd_ctx* ctx, double dt, const double* dtp = nullptr) {
     int rc = alloc_f32(ctx, &ctx->U32[1]);
     if (rc) return rc;
     if ((ctx->sw & kSwShr) && !ctx->FT64) {
@@ -347,6 +348,9 @@ int fused32_step(mhd_ctx* ctx, double dt) {
         a.zf = reinterpret_cast<const float*>(ctx->d_bg + 4 * nz);
         a.gdt = gam[s] * dt;
         a.zdt = zet[s] * dt;
+        a.dtp = dtp;
+        a.gam = gam[s];
+        a.zet = zet[s];
         a.substage = s;
         cudaEvent_t* ev = nullptr;
         if (ctx->profiling) {
@@ -838,8 +842,8 @@ int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach) {
     if (!ctx) return MHD_ERR_INVALID;
     const bool mag = (ctx->sw & kSwMag) != 0;
     const int nz = ctx->g.nz;
-    int e = ctx->fp32 ? cfl32(mag, ctx->g, ctx->c, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->d_bg, ctx->d_bg + nz,
-                              ctx->red, ctx->red_blocks, ctx->d_out, ctx->stream)
+    int e = ctx->fp32 ? cfl32_rows(mag, ctx->g, ctx->c, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->d_bg,
+                                   ctx->d_bg + nz, ctx->red, ctx->red_blocks, ctx->d_out, ctx->stream)
                       : parity_cfl(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks,
                                    ctx->d_out, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "CFL launch");
@@ -906,9 +910,9 @@ int mhd_steps(mhd_ctx* ctx, int n, double dt) {
 int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out) {
     if (!ctx || n < 0) return MHD_ERR_INVALID;
     if (out) memset(out, 0, sizeof(*out));
-    if (ctx->fp32 || ctx->prm.path == MHD_PATH_PARITY || ctxops::plume_time_dependent(ctx)) {
-        // these paths read the CFL dt back every step (a time-dependent plume
-        // needs TIMT on the host before each step)
+    if (ctx->prm.path == MHD_PATH_PARITY || ctxops::plume_time_dependent(ctx)) {
+        // these read the CFL dt back every step (the unfused sequence takes
+        // host scalars; a time-dependent plume needs TIMT on the host)
         mhd_diag d{};
         for (int s = 0; s < n; s++) {
             const int rc = mhd_step(ctx, 0.0, &d);
@@ -926,16 +930,23 @@ int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out) {
     h[7] = ctx->timc;
     CK(cudaMemcpyAsync(rec, h, sizeof(double) * kDtRecord, cudaMemcpyHostToDevice, ctx->stream));
     const bool mag = (ctx->sw & kSwMag) != 0;
+    const int nz = ctx->g.nz;
     for (int s = 0; s < n; s++) {
-        int rc = ensure_u1(ctx);
-        if (!rc) rc = sync_zghosts(ctx);
-        if (rc) return rc;
-        const int e = cfl_dt_on_device(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red,
-                                       ctx->red_blocks, rec, ctx->stream);
+        int e;
+        if (ctx->fp32) {
+            e = cfl32_dt_on_device(mag, ctx->g, ctx->c, fields32_of(ctx, ctx->U32[ctx->cur]), ctx->d_bg,
+                                   ctx->d_bg + nz, ctx->red, ctx->red_blocks, rec, ctx->stream);
+        } else {
+            int rc = ensure_u1(ctx);
+            if (!rc) rc = sync_zghosts(ctx);
+            if (rc) return rc;
+            e = cfl_dt_on_device(mag, ctx->g, ctx->c, fields_of(ctx, ctx->U[ctx->cur]), ctx->red, ctx->red_blocks,
+                                 rec, ctx->stream);
+        }
         if (e) return cuda_fail(ctx, (cudaError_t)e, "CFL launch");
         // BCON reads TIMT only through cos(0 * TIMT) = 1 (3dmhdsub.h:725,732,824), so the
         // host's TIMT at the call stands in for the device's
-        rc = fused_step(ctx, 0.0, rec);
+        const int rc = ctx->fp32 ? fused32_step(ctx, 0.0, rec) : fused_step(ctx, 0.0, rec);
         if (rc) return rc;
     }
     CK(cudaMemcpyAsync(h, rec, sizeof(double) * kDtRecord, cudaMemcpyDeviceToHost, ctx->stream));

@@ -173,6 +173,9 @@ struct Fused32Args {
     double gdt, zdt;
     double timt;
     int substage;
+    // device time-step record of mhd_steps_cfl (as FusedArgs)
+    const double* dtp;
+    double gam, zet;
 };
 int fused32_substage(unsigned sw, const Fused32Args& a, cudaStream_t st);
 int fused32_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const double* bgR,
@@ -185,8 +188,12 @@ int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* ite
                            cudaStream_t st);
 int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm);
 int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st);
-int cfl32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT, double* partials,
-          int max_blocks, double* out5, cudaStream_t st);
+// CFL reduction of an FP32-storage state (the FP64 row kernel on the widened
+// fields): out5 as parity_cfl, or the device time-step record as cfl_dt_on_device
+int cfl32_rows(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
+               double* partials, int max_blocks, double* out5, cudaStream_t st);
+int cfl32_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
+                       double* partials, int max_blocks, double* rec, cudaStream_t st);
 int diag32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
            double* partials, int max_blocks, double* out4, cudaStream_t st);
 

@@ -125,6 +125,11 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
     const float tmpc = (float)(c.OCV / c.REPR);
     const float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
     const float omz = (float)c.OMZ, omx = (float)c.OMX;
+    // RK coefficients: from the host, or from the device time-step record; a
+    // halted record (dt below 1e-8) turns the substage into a copy of the state
+    const double gdt = a.dtp ? a.gam * a.dtp[0] : a.gdt;
+    const double zdt = a.dtp ? a.zet * a.dtp[0] : a.zdt;
+    const bool halted = a.dtp && a.dtp[3] != 0.0;
 
     load_plane32<SW>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
     load_plane32<SW>(a, ring, zb % 3, zb, x0, y0);
@@ -312,12 +317,14 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 // and by BCON), so substage 1 starts from it instead of from the
                 // FP32 copy: step_block_ZETA0 without the FP32 rounding.
                 const double zf = a.Z.p[f][i];
-                const double un = fma(a.gdt, fl[f], zf);
+                const double un = halted ? zf : fma(gdt, fl[f], zf);
                 const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
                 store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
-                a.Z.p[f][i] = (a.substage < 2) ? fma(a.zdt, fl[f], un) : un;
+                a.Z.p[f][i] = (a.substage < 2 && !halted) ? fma(zdt, fl[f], un) : un;
             }
-            if constexpr (SW::lShr) a.FT[i] = ftd;
+            if constexpr (SW::lShr) {
+                if (!halted) a.FT[i] = ftd;
+            }
         }
         __syncthreads();
         if (z + 2 <= ze) load_plane32<SW>(a, ring, (z + 2) % 3, z + 2, x0, y0);
@@ -582,66 +589,6 @@ __device__ __forceinline__ double rec(const Fields8f& U, const double* bg, int f
     return bg ? v + bg[z] : v;
 }
 
-// CFL candidates of step() (3dmhdsub.h:36-106) in FP64 from the reconstructed state.
-template <bool MAG>
-__global__ void k_cfl32(Grid g, Consts c, Fields8f U, const double* bgR, const double* bgT, double* part) {
-    const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
-    const long long ncell = (long long)nPx * nPy * nPz;
-    const double OGAMMA = 1.0f / c.GAMMA;
-    double um = 0.0, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int x = 1 + (int)(t % nPx);
-        const int y = 1 + (int)((t / nPx) % nPy);
-        const int z = 1 + (int)(t / ((long long)nPx * nPy));
-        const long long i = z * g.sz + y * g.sy + x;
-        const double ru = U.p[S_RU][i], rv = U.p[S_RV][i], rw = U.p[S_RW][i];
-        const double ro = rec(U, bgR, S_RO, i, z), tt = rec(U, bgT, S_TT, i, z);
-        double uu = (ru * ru + rv * rv + rw * rw) / (ro * ro);
-        um = fmax(um, OGAMMA * uu / tt);
-        double b2 = 0.0;
-        if constexpr (MAG) {
-            const double bx = U.p[S_BX][i], by = U.p[S_BY][i], bz = U.p[S_BZ][i];
-            b2 = (bx * bx + by * by + bz * bz) * c.OBETA / ro;
-            uu += c.GAMMA * tt + b2 + 2.0 * sqrt(uu * (c.GAMMA * tt + b2));
-        } else {
-            uu += c.GAMMA * tt + 2.0 * sqrt(c.GAMMA * uu * tt);
-        }
-        double DD = fmin(c.DDY[y], c.DDZ[z]);
-        if (g.nx > 3) DD = fmin(DD, c.DDX[x]);
-        w0 = fmin(w0, DD / sqrt(uu));
-        w1 = fmin(w1, 0.5 * DD * DD * c.REPR * c.CV * ro / c.RKAPA[z]);
-        w2 = fmin(w2, 0.375 * DD * DD * c.RE * ro);
-        if constexpr (MAG) w3 = fmin(w3, 0.5 * DD * DD * c.RM);
-    }
-    __shared__ double s[5][kRedThreads];
-    s[0][threadIdx.x] = um;
-    s[1][threadIdx.x] = w0;
-    s[2][threadIdx.x] = w1;
-    s[3][threadIdx.x] = w2;
-    s[4][threadIdx.x] = w3;
-    __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-        if ((int)threadIdx.x < h) {
-            s[0][threadIdx.x] = fmax(s[0][threadIdx.x], s[0][threadIdx.x + h]);
-            for (int k = 1; k < 5; k++) s[k][threadIdx.x] = fmin(s[k][threadIdx.x], s[k][threadIdx.x + h]);
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 5; k++) part[(long long)k * gridDim.x + blockIdx.x] = s[k][0];
-}
-
-__global__ void k_cfl32_finish(const double* part, int nb, double* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double v[5] = {0.0, 1e99, 1e99, 1e99, 1e99};
-    for (int b = 0; b < nb; b++) {
-        v[0] = fmax(v[0], part[b]);
-        for (int k = 1; k < 5; k++) v[k] = fmin(v[k], part[(long long)k * nb + b]);
-    }
-    for (int k = 0; k < 5; k++) out[k] = v[k];
-}
-
 // Mass, energy, max |div B| and flags in FP64 from the reconstructed state
 // (same definitions as the FP64 diagnostics in mhd_diag.cu).
 template <bool MAG>
@@ -721,14 +668,6 @@ int red_blocks(const Grid& g, int cap) {
 
 }  // namespace
 
-int cfl32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT, double* partials,
-          int max_blocks, double* out5, cudaStream_t st) {
-    const int nb = red_blocks(g, max_blocks);
-    if (mag) k_cfl32<true><<<nb, kRedThreads, 0, st>>>(g, c, U, bgR, bgT, partials);
-    else k_cfl32<false><<<nb, kRedThreads, 0, st>>>(g, c, U, bgR, bgT, partials);
-    k_cfl32_finish<<<1, 32, 0, st>>>(partials, nb, out5);
-    return (int)cudaGetLastError();
-}
 
 int diag32(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
            double* partials, int max_blocks, double* out4, cudaStream_t st) {

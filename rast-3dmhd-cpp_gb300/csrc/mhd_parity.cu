@@ -501,15 +501,31 @@ __device__ __forceinline__ double cfl_a1(const Consts& c, double DD, double ro, 
 __device__ __forceinline__ double cfl_a2(const Consts& c, double DD, double ro) { return 0.375f * DD * DD * c.RE * ro; }
 __device__ __forceinline__ double cfl_a3(const Consts& c, double DD) { return 0.5f * DD * DD * c.RM; }
 
-// mc and the fast-mode speed^2 UU' of cell i
-template <bool MAG>
-__device__ __forceinline__ void cfl_speeds(const Consts& c, const Fields8& U, long long i, double OGAMMA, double& mc,
+// Field access of the CFL reduction: FP64 state, or FP32-storage state
+// (deviations from the FP64 profiles rho0(z), T0(z)) widened to FP64.
+struct CflFields64 {
+    Fields8 U;
+    __device__ double f(int k, long long i) const { return U.p[k][i]; }
+    __device__ double ro(long long i, int) const { return U.p[S_RO][i]; }
+    __device__ double tt(long long i, int) const { return U.p[S_TT][i]; }
+};
+struct CflFields32 {
+    Fields8f U;
+    const double *bgR, *bgT;
+    __device__ double f(int k, long long i) const { return widen_f32(U.p[k][i]); }
+    __device__ double ro(long long i, int z) const { return bgR[z] + widen_f32(U.p[S_RO][i]); }
+    __device__ double tt(long long i, int z) const { return bgT[z] + widen_f32(U.p[S_TT][i]); }
+};
+
+// mc and the fast-mode speed^2 UU' of cell i (plane z)
+template <bool MAG, class FA>
+__device__ __forceinline__ void cfl_speeds(const Consts& c, const FA& U, long long i, int z, double OGAMMA, double& mc,
                                            double& uu) {
-    const double ru = U.p[S_RU][i], rv = U.p[S_RV][i], rw = U.p[S_RW][i], ro = U.p[S_RO][i], tt = U.p[S_TT][i];
+    const double ru = U.f(S_RU, i), rv = U.f(S_RV, i), rw = U.f(S_RW, i), ro = U.ro(i, z), tt = U.tt(i, z);
     double UU = (ru * ru + rv * rv + rw * rw) / (ro * ro);
     mc = OGAMMA * UU / tt;
     if constexpr (MAG) {
-        const double bx = U.p[S_BX][i], by = U.p[S_BY][i], bz = U.p[S_BZ][i];
+        const double bx = U.f(S_BX, i), by = U.f(S_BY, i), bz = U.f(S_BZ, i);
         UU += c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro +
               2.0f * sqrt(UU * (c.GAMMA * tt + (bx * bx + by * by + bz * bz) * c.OBETA / ro));
     } else {
@@ -519,16 +535,16 @@ __device__ __forceinline__ void cfl_speeds(const Consts& c, const Fields8& U, lo
 }
 
 // all five candidates of cell (x, y, z), folded into the running extrema
-template <bool MAG>
-__device__ __forceinline__ void cfl_cell(const Grid& g, const Consts& c, const Fields8& U, int x, int y, int z,
+template <bool MAG, class FA>
+__device__ __forceinline__ void cfl_cell(const Grid& g, const Consts& c, const FA& U, int x, int y, int z,
                                          double OGAMMA, double& um, double& w0, double& w1, double& w2, double& w3) {
     const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
     double mc, UU;
-    cfl_speeds<MAG>(c, U, i, OGAMMA, mc, UU);
+    cfl_speeds<MAG>(c, U, i, z, OGAMMA, mc, UU);
     um = (um < mc) ? mc : um;
     double DD = cfl_dd_yz(c, y, z);
     if (g.nx > 3) DD = (c.DDX[x] < DD) ? c.DDX[x] : DD;
-    const double ro = U.p[S_RO][i];
+    const double ro = U.ro(i, z);
     const double a0 = DD / sqrt(UU);
     const double a1 = cfl_a1(c, DD, ro, z);
     const double a2 = cfl_a2(c, DD, ro);
@@ -586,10 +602,10 @@ __device__ __forceinline__ bool nonzero_bits(double d) {
 
 // FP32 estimates of cell i's fast-mode candidate a0 and of mc (both certified
 // to 1.2e-6 when `ok`), and whether its momenta are not all exactly zero.
-template <bool MAG>
-__device__ __forceinline__ void cfl_estimate(const Fields8& U, long long i, float ddf, float gam_f, float obeta_f,
+template <bool MAG, class FA>
+__device__ __forceinline__ void cfl_estimate(const FA& U, long long i, int z, float ddf, float gam_f, float obeta_f,
                                              double rod, float& a0, float& mc, bool& ok, bool& nz) {
-    const double rud = U.p[S_RU][i], rvd = U.p[S_RV][i], rwd = U.p[S_RW][i], ttd = U.p[S_TT][i];
+    const double rud = U.f(S_RU, i), rvd = U.f(S_RV, i), rwd = U.f(S_RW, i), ttd = U.tt(i, z);
     nz = nonzero_bits(rud) || nonzero_bits(rvd) || nonzero_bits(rwd);
     const float ru = trunc_to_f32(rud), rv = trunc_to_f32(rvd), rw = trunc_to_f32(rwd);
     const float ro = trunc_to_f32(rod), tt = trunc_to_f32(ttd);
@@ -598,7 +614,7 @@ __device__ __forceinline__ void cfl_estimate(const Fields8& U, long long i, floa
     const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
     float G = __fmul_rn(gam_f, tt);
     if constexpr (MAG) {
-        const float bx = trunc_to_f32(U.p[S_BX][i]), by = trunc_to_f32(U.p[S_BY][i]), bz = trunc_to_f32(U.p[S_BZ][i]);
+        const float bx = trunc_to_f32(U.f(S_BX, i)), by = trunc_to_f32(U.f(S_BY, i)), bz = trunc_to_f32(U.f(S_BZ, i));
         const float b2 = __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
         G = __fadd_rn(G, __fmul_rn(__fmul_rn(obeta_f, b2), ir));
     }
@@ -623,8 +639,8 @@ __device__ __forceinline__ bool cfl_fast_row(const Grid& g, const Consts& c, int
 // keys (0 = nothing seen).  Any estimate that some certified cell attains is a
 // valid filter base, so the row kernel may start from these.
 constexpr int kCflSeedStride = 8;
-template <bool MAG>
-__global__ void k_cfl_seed(Grid g, Consts c, Fields8 U, unsigned* seed) {
+template <bool MAG, class FA>
+__global__ void k_cfl_seed(Grid g, Consts c, FA U, unsigned* seed) {
     const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
     const long long nrows = ((long long)nPy * nPz + kCflSeedStride - 1) / kCflSeedStride;
     const int lane = threadIdx.x & 31;
@@ -641,7 +657,7 @@ __global__ void k_cfl_seed(Grid g, Consts c, Fields8 U, unsigned* seed) {
         for (int x = 1 + lane; x <= nPx; x += 32) {
             float a0, mc;
             bool ok, nz;
-            cfl_estimate<MAG>(U, row + x, ddf, gam_f, obeta_f, U.p[S_RO][row + x], a0, mc, ok, nz);
+            cfl_estimate<MAG>(U, row + x, z, ddf, gam_f, obeta_f, U.ro(row + x, z), a0, mc, ok, nz);
             if (ok) {
                 best_a = fminf(best_a, a0);
                 if (nz) best_m = fmaxf(best_m, mc);
@@ -685,8 +701,8 @@ constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x t
 // evaluated exactly, and the result equals the cell-by-cell reduction bit for
 // bit; after the first passes only new near-extremes are evaluated.  Rows with varying DD, and launches whose constants break the
 // monotonicity (non-positive factors), evaluate every cell exactly.
-template <bool MAG>
-__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, Fields8 U, const unsigned* seed,
+template <bool MAG, class FA>
+__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, FA U, const unsigned* seed,
                                                              double* part) {
     __shared__ int list[kCflWarps][32 * kCflK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -721,11 +737,11 @@ __global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, F
                 if (x > nPx) continue;
                 valid |= 1u << k;
                 const long long i = row + x;
-                const double rod = U.p[S_RO][i];
+                const double rod = U.ro(i, z);
                 mro = (rod < mro) ? rod : mro;
                 float a0, mc;
                 bool ok, nz;
-                cfl_estimate<MAG>(U, i, ddf, gam_f, obeta_f, rod, a0, mc, ok, nz);
+                cfl_estimate<MAG>(U, i, z, ddf, gam_f, obeta_f, rod, a0, mc, ok, nz);
                 aA[k] = a0;
                 mA[k] = mc;
                 if (ok) {
@@ -757,7 +773,7 @@ __global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, F
             for (int j = lane; j < n; j += 32) {
                 const int x = list[wid][j];
                 double mc, UU;
-                cfl_speeds<MAG>(c, U, row + x, OGAMMA, mc, UU);
+                cfl_speeds<MAG>(c, U, row + x, z, OGAMMA, mc, UU);
                 um = (um < mc) ? mc : um;
                 const double a0 = DDyz / sqrt(UU);
                 w0 = (a0 < w0) ? a0 : w0;
@@ -785,16 +801,17 @@ __global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, F
 // Launch the row reduction with one wave of resident blocks (each warp then
 // sees many rows, so its running estimates filter most cells); returns the
 // number of partial blocks.
-int launch_cfl_rows(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+template <class FA>
+int launch_cfl_rows_t(bool mag, const Grid& g, const Consts& c, FA U, double* partials, int max_blocks,
                     cudaStream_t st) {
-    static int wave[2] = {0, 0};
+    static int wave[2] = {0, 0};  // per accessor type
     int& w = wave[mag ? 1 : 0];
     if (!w) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (mag) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<true>, kCflWarps * 32, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<false>, kCflWarps * 32, 0);
+        if (mag) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<true, FA>, kCflWarps * 32, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfl_rows<false, FA>, kCflWarps * 32, 0);
         w = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
     }
     const long long nrows = (long long)(g.ny - 2) * (g.nz - 2);
@@ -810,13 +827,17 @@ int launch_cfl_rows(bool mag, const Grid& g, const Consts& c, Fields8 U, double*
     if (sb > w) sb = w;
     if (sb < 1) sb = 1;
     if (mag) {
-        k_cfl_seed<true><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
-        k_cfl_rows<true><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
+        k_cfl_seed<true, FA><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
+        k_cfl_rows<true, FA><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
     } else {
-        k_cfl_seed<false><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
-        k_cfl_rows<false><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
+        k_cfl_seed<false, FA><<<(int)sb, 256, 0, st>>>(g, c, U, seed);
+        k_cfl_rows<false, FA><<<(int)nb, kCflWarps * 32, 0, st>>>(g, c, U, seed, partials);
     }
     return (int)nb;
+}
+int launch_cfl_rows(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
+                    cudaStream_t st) {
+    return launch_cfl_rows_t(mag, g, c, CflFields64{U}, partials, max_blocks, st);
 }
 
 // Reduce the per-block CFL partials (5 x nb) into v[0] = max UMACH^2
@@ -1006,6 +1027,20 @@ int lrem_profiles(const Grid& g, const Consts& c, const double* TT, double* buf,
     if (exact) k_lrem_ttm_exact<<<(g.nz + 63) / 64, 64, 0, st>>>(g, TT, ttm);
     else k_lrem_ttm_fast<<<g.nz, 256, 0, st>>>(g, TT, ttm);
     k_lrem_hrad<<<(g.nz + 63) / 64, 64, 0, st>>>(g, c, ttm, hrad, G);
+    return (int)cudaGetLastError();
+}
+
+int cfl32_rows(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
+               double* partials, int max_blocks, double* out5, cudaStream_t st) {
+    const int nb = launch_cfl_rows_t(mag, g, c, CflFields32{U, bgR, bgT}, partials, max_blocks, st);
+    k_cfl_finish<<<1, 256, 0, st>>>(partials, nb, out5);
+    return (int)cudaGetLastError();
+}
+
+int cfl32_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,
+                       double* partials, int max_blocks, double* rec, cudaStream_t st) {
+    const int nb = launch_cfl_rows_t(mag, g, c, CflFields32{U, bgR, bgT}, partials, max_blocks, st);
+    k_cfl_record<<<1, 256, 0, st>>>(partials, nb, c.SFF, mag ? 1 : 0, rec);
     return (int)cudaGetLastError();
 }
 

@@ -96,6 +96,43 @@ def test_halt_leaves_state_unchanged():
     sim.close()
 
 
+def test_fp32_device_record_equals_host_cfl_steps():
+    """FP32 storage: 12 steps with the dt kept on the device equal, bit for
+    bit, 12 steps whose CFL dt went through the host; the dt is the FP64
+    reduction over the widened FP32 state."""
+    case = Case(nPx=40, nPy=32, nPz=24, lMag=True, lRot=True, seed=8, name="cfl32")
+    st0 = initial_state(case)
+    a, b = Simulation(case, precision="fp32"), Simulation(case, precision="fp32")
+    for s in (a, b):
+        s.upload_state(st0)
+        s.communicate()
+    _, da = a.steps_cfl(12)
+    for _ in range(12):
+        db = b.step(0.0)
+    assert da["dt"] == db["dt"] and da["timt"] == db["timt"] and da["nit"] == db["nit"] == 12
+    ga, gb = a.download_state(), b.download_state()
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(ga[k], gb[k]), k
+    a.close()
+    b.close()
+
+
+def test_fp32_halt_leaves_state_unchanged():
+    case = Case(nPx=32, nPy=32, nPz=16, lMag=True, seed=9, SFF=1e-12, name="halt32")
+    sim = Simulation(case, precision="fp32")
+    sim.upload_state(initial_state(case))
+    sim.communicate()
+    sim.step(case.dt)
+    before = sim.download_state()
+    st, d = sim.steps_cfl(4, check=False)
+    assert st == abi.MHD_ERR_DT_TOO_SMALL and d["nit"] == 1
+    after = sim.download_state()
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(before[k], after[k]), k
+    sim.step(case.dt)
+    sim.close()
+
+
 def test_fp32_storage_steps_cfl():
     """The FP32-storage form takes the CFL dt from its FP64 reduction; its
     first dt equals the FP64 one to the FP32 storage rounding."""
