@@ -702,7 +702,7 @@ constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x t
 // bit; after the first passes only new near-extremes are evaluated.  Rows with varying DD, and launches whose constants break the
 // monotonicity (non-positive factors), evaluate every cell exactly.
 template <bool MAG, class FA>
-__global__ void __launch_bounds__(kCflWarps * 32) k_cfl_rows(Grid g, Consts c, FA U, const unsigned* seed,
+__global__ void __launch_bounds__(kCflWarps * 32, 3) k_cfl_rows(Grid g, Consts c, FA U, const unsigned* seed,
                                                              double* part) {
     __shared__ int list[kCflWarps][32 * kCflK];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
