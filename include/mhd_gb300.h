@@ -256,6 +256,32 @@ int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double dt);
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
 int mhd_sync(mhd_ctx* ctx);
 
+/* The run parameters Static() reads beyond mhd_params (par[8..10],
+ * par[18..22], 3dmhd.cpp:409-423) and the rank grid of the run: the Bx layer
+ * depends on the z split (nPEz); nPEy only has to divide nPy. */
+typedef struct mhd_static_params {
+    int nPEy, nPEz;       /* rank grid of the run being started (3dmhdparam.h:18-19) */
+    int reserved_i[2];
+    double zMax;          /* depth of the box; Static() integrates on z = zz zMax */
+    double PZP, SIGMA;    /* conductivity step position and width (0: none) */
+    double POLYS;         /* polytropic index of the lower layer */
+    double AMPT;          /* temperature (lShr: RV) noise amplitude */
+    double AMPB, BFH, BZP;/* lMag: Bx layer amplitude, FWHM, centre */
+    const double* ZEE;    /* nPz + 2 z coordinates, ghosts included (length nz) */
+    double reserved_d[4];
+} mhd_static_params;
+
+/* The reference's fresh-start initial state (Static(), 3dmhdphsic.h:549-763,
+ * followed by communicate() as in 3dmhd.cpp:111-142), computed on the host:
+ * `state` receives nf x nz x ny x nx doubles, field-major as in
+ * mhd_upload_state, bit-identical to the reference run with the same
+ * parameters and rank grid.  Uses THETA, GRAV, BETA, the switches and the
+ * grid of `p` only; needs no context and no GPU.  MHD_ERR_UNSUPPORTED with
+ * MHD_SW_LREM (that background is a tabulated stellar model); flux tubes
+ * (nTube >= 1) are not built: with lMag and AMPB = 0 the field is zero, as
+ * tube() gives for nTube = 0. */
+int mhd_static_state(const mhd_params* p, const mhd_static_params* s, double* state);
+
 /* Self-check: the integer-pipe float<->double conversions the FP32-storage
  * kernels use against the hardware conversions, on n test patterns of seed;
  * *mismatches receives the number of differing results (0 expected). */

@@ -19,6 +19,10 @@
  *   mode 3  one RK3 substage                            (3dmhdsub.h:116-124)
  *   mode 4  as mode 1, then the reference's dumpData() writes record 0 of
  *           "<argv[3]>.dat0.PPPP" per rank                (3dmhdio.h:20-35)
+ *   mode 5  the fresh-start initial state: Static(), then communicate()
+ *           again (3dmhdphsic.h:549-763, 3dmhd.cpp:111-142); the input
+ *           state should be zero (Static() leaves some planes of BX as
+ *           it finds them)
  * and every rank writes the part of the global arrays it owns into the
  * output file, so the output is the single-domain equivalent state.
  */
@@ -240,6 +244,10 @@ int main(int argc, char** argv) {
             dt_hist.push_back(DT);
         }
         dumpData(std::string(argv[3]) + ".dat0." + PEextn(), 0);
+    } else if (h.mode == 5) {
+        /* a fresh start: Static() then communicate(), as main() (3dmhd.cpp:111-142) */
+        Static();
+        communicate();
     } else if (h.mode == 3) {
         step_block_ZETA0(FORRANGE);
         fluxes(FORRANGE);

@@ -111,6 +111,12 @@ def set_header(case: Case) -> str:
     par = {0: case.RE, 1: case.PR, 2: case.THETA, 3: case.GRAV, 4: case.RY, 5: case.ANG,
            6: case.RM, 7: case.BETA, 11: case.TP, 12: case.TC, 13: case.XP, 14: case.YP, 15: case.ZP,
            16: case.xMax, 17: case.yMax, 18: case.zMax, 52: case.QFH, 53: case.GAMMA, 54: case.HH}
+    # Static()'s model (3dmhd.cpp:409-423), written only when set so that the
+    # headers of the other cases stay as they were
+    for k, v in ((8, case.PZP), (9, case.SIGMA), (10, case.POLYS), (19, case.AMPT), (20, case.AMPB),
+                 (21, case.BFH), (22, case.BZP)):
+        if v != 0.0:
+            par[k] = v
     lines = "\n".join(f"    par[{k}] = {_hexf(v)};" for k, v in sorted(par.items()))
     return f"""#ifndef _3DMHD_SET_H_
 #define _3DMHD_SET_H_
@@ -175,7 +181,7 @@ def build(case: Case) -> Path:
 # ---------------------------------------------------------------------------
 # harness input / output files
 # ---------------------------------------------------------------------------
-MODES = {"fluxes": 0, "steps": 1, "cfl": 2, "substage": 3, "dump": 4}
+MODES = {"fluxes": 0, "steps": 1, "cfl": 2, "substage": 3, "dump": 4, "static": 5}
 
 
 def write_input(path: Path, case: Case, state: dict, mode: str, nsteps: int,

@@ -38,6 +38,7 @@ UNITS = [
     ("mhd_init.cu", "mhd_init", []),
     ("mhd_pipeline.cu", "mhd_pipeline", []),
     ("mhd_selftest.cu", "mhd_selftest", []),
+    ("mhd_static.cu", "mhd_static", []),
 ]
 
 

@@ -13,6 +13,7 @@ PKG = Path(__file__).resolve().parent.parent.parent   # rast-3dmhd-cpp_gb300/
 LIB_PATH = PKG / "lib" / "libmhd_gb300.so"
 
 MHD_OK = 0
+MHD_ERR_INVALID, MHD_ERR_UNSUPPORTED = -1, -2
 MHD_ERR_NUMERIC, MHD_ERR_DT_TOO_SMALL = -4, -5
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported configuration", -3: "CUDA error",
           -4: "non-finite or non-positive state", -5: "DT too small", -6: "out of device memory",
@@ -59,6 +60,12 @@ class MhdDiag(C.Structure):
 class MhdPlume(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("XP", "YP", "ZP", "HH", "TC", "QFH")] + \
                [(n, C.POINTER(C.c_double)) for n in ("EXX", "WYY", "ZEE")]
+
+
+class MhdStaticParams(C.Structure):
+    _fields_ = [("nPEy", C.c_int), ("nPEz", C.c_int), ("reserved_i", C.c_int * 2)] + \
+               [(n, C.c_double) for n in ("zMax", "PZP", "SIGMA", "POLYS", "AMPT", "AMPB", "BFH", "BZP")] + \
+               [("ZEE", C.POINTER(C.c_double)), ("reserved_d", C.c_double * 4)]
 
 
 NOALLOC_MAX_CELLS = 393216
@@ -110,6 +117,7 @@ SIGNATURES = {
     "mhd_step_host": [C.c_void_p, _DP, _DP, C.c_double],
     "mhd_set_plume": [C.c_void_p, C.POINTER(MhdPlume)],
     "mhd_selftest_convert": [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
+    "mhd_static_state": [C.POINTER(MhdParams), C.POINTER(MhdStaticParams), _DP],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],
     "mhd_batch_create": [C.POINTER(C.c_void_p), _DP, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)],

@@ -70,6 +70,16 @@ class Case:
     xMax: float = 6.0
     yMax: float = 6.0
     zMax: float = 2.0
+    # fresh-start model of Static() (3dmhdphsic.h:549-763; par[8..10], par[19..22]):
+    # conductivity step at zz = PZP of width SIGMA to the polytrope of index
+    # POLYS, temperature noise AMPT, Gaussian Bx layer AMPB of FWHM BFH at BZP
+    PZP: float = 0.0
+    SIGMA: float = 0.0
+    POLYS: float = 0.0
+    AMPT: float = 0.0
+    AMPB: float = 0.0
+    BFH: float = 0.0
+    BZP: float = 0.0
     GAMMA: float = GAMMA_DEFAULT
     SFF: float = f32(0.8)   # 3dmhdparam.h:111
     z_stretch: float = 1.5  # tanh stretch factor; 0 gives the reference's uniform grid
@@ -327,6 +337,22 @@ def lrem_cases() -> dict[str, Case]:
     return {
         "lrem_fixedT": Case(name="lrem_fixedT", iTCon=0, izCon=0, TU=1.05, **base),
         "lrem_flux": Case(name="lrem_flux", lMag=False, lRot=True, iTCon=1, izCon=1, DZTU=-0.03, DZTB=0.02, **base),
+    }
+
+
+def static_cases() -> dict[str, Case]:
+    """Fresh-start cases of Static(): the polytrope with a Bx layer and noise
+    on 2 x 2 ranks, the conductivity step (PZP, SIGMA, POLYS) on 1 x 4 ranks
+    with a layer that meets the z-rank edges, and lShr's RV noise with the
+    zero field of tube() (nTube = 0)."""
+    base = dict(nPx=12, nPy=8, nPz=8, seed=7)
+    return {
+        "static_layer": Case(name="static_layer", nPEy=2, nPEz=2, AMPT=0.02, AMPB=0.1, BFH=0.5, BZP=1.2, **base),
+        "static_kappa": Case(name="static_kappa", lMag=True, nPEy=1, nPEz=4, PZP=0.6, SIGMA=0.1, POLYS=1.5,
+                             AMPT=0.05, AMPB=0.3, BFH=0.8, BZP=0.9, **base),
+        "static_shr": Case(name="static_shr", lShr=True, lRot=True, nPEy=2, nPEz=2, AMPT=0.03, **base),
+        "static_hydro": Case(name="static_hydro", lMag=False, nPEy=4, nPEz=2, PZP=0.3, SIGMA=0.05, POLYS=1.0,
+                             AMPT=0.01, **base),
     }
 
 

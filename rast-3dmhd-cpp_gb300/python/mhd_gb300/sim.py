@@ -41,6 +41,26 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def static_state(case: Case, nPEy: int | None = None, nPEz: int | None = None) -> dict:
+    """The reference's fresh-start state for ``case`` (Static() and
+    communicate(), 3dmhdphsic.h:549-763, 3dmhd.cpp:111-142) from
+    mhd_static_state: a dict field -> (nz, ny, nx) array.  The Bx layer
+    depends on the z split of the run reproduced (default: the case's
+    nPEy x nPEz).  Host computation; no GPU is needed."""
+    L = abi.load()
+    p, keep = params_for(case)
+    sp = abi.MhdStaticParams()
+    sp.nPEy = case.nPEy if nPEy is None else nPEy
+    sp.nPEz = case.nPEz if nPEz is None else nPEz
+    for k in ("zMax", "PZP", "SIGMA", "POLYS", "AMPT", "AMPB", "BFH", "BZP"):
+        setattr(sp, k, float(getattr(case, k)))
+    zee = np.ascontiguousarray(coordinates(case)[2], dtype=np.float64)
+    sp.ZEE = _dp(zee)
+    out = np.empty((case.nfields,) + case.shape, dtype=np.float64)
+    abi.check(L.mhd_static_state(C.byref(p), C.byref(sp), _dp(out)))
+    return {k: out[i] for i, k in enumerate(STATE_FIELDS[:case.nfields])}
+
+
 class Simulation:
     """One device-resident 3dmhd instance."""
 

@@ -17,10 +17,16 @@ seeded initial state and stores, as <case>.npz:
   cfl2_*    the state after 2 steps of the reference step() with its CFL dt,
             and cfl2_dt the two time steps (two cases only)
 plus config0_digest.json: SHA-256 digests of the 64x64x32 MHD run of the
-plain-method configuration after 100 fixed-dt steps (too large to store).
+plain-method configuration after 100 fixed-dt steps (too large to store),
+and for every fresh-start case of mhd_gb300.case.static_cases the state the
+reference's Static() and communicate() build (<case>.npz, all fields,
+ghosts included, with the z coordinates it was given).
+
+    python tests/golden/make_golden.py --only static   # just the Static() fixtures
 """
 from __future__ import annotations
 
+import argparse
 import hashlib
 import json
 import sys
@@ -34,8 +40,8 @@ sys.path.insert(0, str(REPO / "oracle"))
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
 
 import refcase  # noqa: E402
-from mhd_gb300.case import (FLUX_FIELDS, STATE_FIELDS, config0, config1, initial_state, metrics,  # noqa: E402
-                            lrem_cases, plume_cases, small_cases)
+from mhd_gb300.case import (FLUX_FIELDS, STATE_FIELDS, config0, config1, coordinates, initial_state,  # noqa: E402
+                            lrem_cases, metrics, plume_cases, small_cases, static_cases)
 
 METRIC_NAMES = ("dxxdx", "d2xxdx2", "DDX", "dyydy", "d2yydy2", "DDY", "dzzdz", "d2zzdz2", "DDZ", "RKAPA", "DKAPA")
 CFL_CASES = ("mhd_fixedT", "hydro_default_bc", "lrem_fixedT", "lrem_flux")
@@ -45,9 +51,31 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
 
 
+def static_fixtures() -> None:
+    """Static() + communicate() of every fresh-start case (harness mode 5);
+    the input state is zero, as the reference's arrays are at a fresh start."""
+    manifest = {}
+    for name, case in static_cases().items():
+        zero = {k: np.zeros(case.shape) for k in STATE_FIELDS}
+        r = refcase.run(case, zero, "static", 0)
+        out = {"ZEE": coordinates(case)[2]}
+        for k in STATE_FIELDS[:case.nfields]:
+            out["static_" + k] = r[k]
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+        manifest[name] = case.to_dict()
+        print("wrote", name)
+    (HERE / "static_cases.json").write_text(json.dumps(manifest, indent=1, sort_keys=True))
+
+
 def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=("all", "static"), default="all")
+    args = ap.parse_args()
     if not refcase.reference_available():
         raise SystemExit(f"reference sources not found under {refcase.REF_DIR}")
+    static_fixtures()
+    if args.only == "static":
+        return
     manifest = {}
     for name, case in list(small_cases().items()) + list(plume_cases().items()) + list(lrem_cases().items()):
         st = initial_state(case)

@@ -1,0 +1,110 @@
+"""The fresh-start initial state (mhd_static_state) against the reference's
+own Static() + communicate() (3dmhdphsic.h:549-763, 3dmhd.cpp:111-142).
+
+The fixtures were written by tests/golden/make_golden.py from the compiled
+reference (harness mode 5) on its rank grid; the library computes the same
+state on the host.  Bit-exact: the background integration, the RAN2 noise and
+the field layer use the reference's expressions, and exp/tanh/log come from
+the same host libm as the fixtures'.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+from mhd_gb300 import abi
+from mhd_gb300.case import STATE_FIELDS, Case, coordinates
+from mhd_gb300.sim import static_state
+
+
+def _cases():
+    return json.loads((GOLDEN / "static_cases.json").read_text())
+
+
+def _case(name) -> Case:
+    return Case(**_cases()[name])
+
+
+@pytest.mark.parametrize("name", sorted(_cases()))
+def test_static_matches_reference_fixture(name):
+    case = _case(name)
+    ref = np.load(GOLDEN / f"{name}.npz")
+    assert np.array_equal(ref["ZEE"], coordinates(case)[2])
+    got = static_state(case)
+    for k in STATE_FIELDS[:case.nfields]:
+        a, b = ref["static_" + k], got[k]
+        bad = np.argwhere(a != b)
+        assert bad.size == 0, f"{name} {k}: {len(bad)} cells differ, first {bad[:3].tolist()}"
+
+
+def test_static_layer_gaps_follow_the_z_ranks():
+    """Static() fills the Bx layer on local planes 2..nRz+1 of every rank
+    (3dmhdphsic.h:685), so plane 1 of every z rank above the lowest has none."""
+    case = _case("static_kappa")  # nPEz = 4, nRz = 2
+    bx = static_state(case)["BX"][:, 4, 4]
+    nrz = case.nPz // case.nPEz
+    for g in range(case.nz):
+        gap = g < 2 or (g <= case.nPz and (g - 1) % nrz == 0)
+        assert (bx[g] == 0.0) == gap, (g, bx.tolist())
+    # another z split moves the gaps; the noise is drawn in global plane,
+    # row, column order on every rank grid (ranks own consecutive planes/rows)
+    mine = static_state(case)
+    assert not np.array_equal(static_state(case, 1, 2)["BX"], mine["BX"])
+    nolayer = case.replace(AMPB=0.0)
+    t = static_state(nolayer, 1, 4)["TT"]
+    for grid in ((1, 2), (2, 2), (4, 1), (8, 8)):
+        assert np.array_equal(static_state(nolayer, *grid)["TT"], t), grid
+    base = case.replace(AMPT=0.0, AMPB=0.0)
+    t1, t2 = static_state(base, 1, 4)["TT"], static_state(base, 2, 2)["TT"]
+    assert np.array_equal(t1, t2)
+    prof = t1[:, 3, 3]
+    assert np.all(np.diff(prof[1:-1]) > 0)  # temperature rises with depth
+    assert np.all(t1 == prof[:, None, None])  # horizontally uniform without noise
+
+
+def test_static_shr_noise_goes_into_rv():
+    case = _case("static_shr")
+    s = static_state(case)
+    assert np.all(s["TT"] == 1.0) and np.all(s["RO"] == 1.0)
+    rv = s["RV"][1:-1, 1:-1, 1:-1]
+    assert np.abs(rv).max() <= 0.5 * case.AMPT and rv.std() > 0.0
+    for k in ("BX", "BY", "BZ", "RU", "RW"):
+        assert not s[k].any()
+    # periodic x / y ghosts
+    assert np.array_equal(s["RV"][:, 0, :], s["RV"][:, -2, :])
+    assert np.array_equal(s["RV"][:, :, -1], s["RV"][:, :, 1])
+
+
+def test_static_rejects_what_is_not_built():
+    import ctypes as C
+    from mhd_gb300.sim import params_for
+    L = abi.load()
+    case = _case("static_layer")
+    out = np.empty((case.nfields,) + case.shape)
+    zee = np.ascontiguousarray(coordinates(case)[2])
+    sp = abi.MhdStaticParams(nPEy=2, nPEz=2, zMax=case.zMax)
+    sp.ZEE = zee.ctypes.data_as(C.POINTER(C.c_double))
+    dp = out.ctypes.data_as(C.POINTER(C.c_double))
+    p, _keep = params_for(case.replace(lRem=True))
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_UNSUPPORTED
+    p, _keep = params_for(case)
+    sp.nPEz = 3  # nPz = 8 does not split over 3 z ranks
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_INVALID
+    sp.nPEz = 2
+    sp.ZEE = None
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_INVALID
+
+
+def test_static_live_reference_other_rank_grid():
+    """The compiled reference on a rank grid no fixture uses (1 x 4 ranks for
+    the 2 x 2 case: other layer gaps), where the reference sources are present."""
+    refcase = pytest.importorskip("refcase")
+    if not refcase.reference_available():
+        pytest.skip("reference sources not present")
+    case = _case("static_layer").replace(nPEy=1, nPEz=4, name="static_layer_1x4")
+    r = refcase.run(case, {k: np.zeros(case.shape) for k in STATE_FIELDS}, "static", 0)
+    got = static_state(case)
+    for k in STATE_FIELDS[:case.nfields]:
+        assert np.array_equal(r[k], got[k]), k
