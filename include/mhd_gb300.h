@@ -261,7 +261,8 @@ int mhd_sync(mhd_ctx* ctx);
  * depends on the z split (nPEz); nPEy only has to divide nPy. */
 typedef struct mhd_static_params {
     int nPEy, nPEz;       /* rank grid of the run being started (3dmhdparam.h:18-19) */
-    int reserved_i[2];
+    int nTube;            /* flux-tube model of tube() (3dmhdparam.h:124); only 0 */
+    int reserved_i;
     double zMax;          /* depth of the box; Static() integrates on z = zz zMax */
     double PZP, SIGMA;    /* conductivity step position and width (0: none) */
     double POLYS;         /* polytropic index of the lower layer */
@@ -276,10 +277,12 @@ typedef struct mhd_static_params {
  * `state` receives nf x nz x ny x nx doubles, field-major as in
  * mhd_upload_state, bit-identical to the reference run with the same
  * parameters and rank grid.  Uses THETA, GRAV, BETA, the switches and the
- * grid of `p` only; needs no context and no GPU.  MHD_ERR_UNSUPPORTED with
- * MHD_SW_LREM (that background is a tabulated stellar model); flux tubes
- * (nTube >= 1) are not built: with lMag and AMPB = 0 the field is zero, as
- * tube() gives for nTube = 0. */
+ * grid of `p` only; needs no context and no GPU.  With lMag and AMPB = 0 the
+ * field is that of tube() with nTube = 0 (zero).  MHD_ERR_UNSUPPORTED with
+ * MHD_SW_LREM (that background is a tabulated stellar model) and for
+ * nTube 1-5, which give the reference no state: 1 and 3 abort in qromb
+ * ("Failure in polint", 3dmhdphsic.h:207-208), 2, 4 and 5 do not compile
+ * (3dmhdphsic.h:843-844, 951-954, 984). */
 int mhd_static_state(const mhd_params* p, const mhd_static_params* s, double* state);
 
 /* Self-check: the integer-pipe float<->double conversions the FP32-storage

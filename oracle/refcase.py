@@ -102,7 +102,7 @@ const double SFF = {_hexf(case.SFF)};
 const double DH = 0, DV = 0;
 const int iWord = 8;
 const int nCol = 0, nRow = 0, nTubes = nCol * nRow;
-#define nTube 0
+#define nTube {case.nTube}
 """
 
 
@@ -114,7 +114,8 @@ def set_header(case: Case) -> str:
     # Static()'s model (3dmhd.cpp:409-423), written only when set so that the
     # headers of the other cases stay as they were
     for k, v in ((8, case.PZP), (9, case.SIGMA), (10, case.POLYS), (19, case.AMPT), (20, case.AMPB),
-                 (21, case.BFH), (22, case.BZP)):
+                 (21, case.BFH), (22, case.BZP), (34, case.XCENT), (35, case.ZCENT), (36, case.R_MAX),
+                 (37, case.C_MT), (38, case.A_TUBE)):
         if v != 0.0:
             par[k] = v
     lines = "\n".join(f"    par[{k}] = {_hexf(v)};" for k, v in sorted(par.items()))

@@ -158,6 +158,9 @@ struct Ran2 {
 extern "C" int mhd_static_state(const mhd_params* p, const mhd_static_params* s, double* state) {
     if (!p || !s || !state || !s->ZEE) return MHD_ERR_INVALID;
     if (p->switches & MHD_SW_LREM) return MHD_ERR_UNSUPPORTED;  // lRem's background is a stellar model
+    if (s->nTube < 0 || s->nTube > 5) return MHD_ERR_INVALID;
+    // tube models 1-5 leave the reference without a state (abort or no build)
+    if (s->nTube != 0 && (p->switches & MHD_SW_LMAG) && s->AMPB == 0.0) return MHD_ERR_UNSUPPORTED;
     const int nPx = p->nPx, nPy = p->nPy, nPz = p->nPz, nPEy = s->nPEy, nPEz = s->nPEz;
     if (nPx < 2 || nPy < 2 || nPz < 4 || nPEy < 1 || nPEz < 1 || nPy % nPEy || nPz % nPEz) return MHD_ERR_INVALID;
     const bool mag = (p->switches & MHD_SW_LMAG) != 0, shr = (p->switches & MHD_SW_LSHR) != 0;

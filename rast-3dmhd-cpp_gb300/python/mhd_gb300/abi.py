@@ -63,7 +63,7 @@ class MhdPlume(C.Structure):
 
 
 class MhdStaticParams(C.Structure):
-    _fields_ = [("nPEy", C.c_int), ("nPEz", C.c_int), ("reserved_i", C.c_int * 2)] + \
+    _fields_ = [("nPEy", C.c_int), ("nPEz", C.c_int), ("nTube", C.c_int), ("reserved_i", C.c_int)] + \
                [(n, C.c_double) for n in ("zMax", "PZP", "SIGMA", "POLYS", "AMPT", "AMPB", "BFH", "BZP")] + \
                [("ZEE", C.POINTER(C.c_double)), ("reserved_d", C.c_double * 4)]
 

@@ -80,6 +80,14 @@ class Case:
     AMPB: float = 0.0
     BFH: float = 0.0
     BZP: float = 0.0
+    # flux-tube model of tube() (3dmhdparam.h:124, 3dmhdphsic.h:765-1027; lMag with
+    # AMPB = 0): model number and par[34..38] (XCENT, ZCENT, R_MAX, C_MT, A)
+    nTube: int = 0
+    XCENT: float = 0.0
+    ZCENT: float = 0.0
+    R_MAX: float = 0.0
+    C_MT: float = 0.0
+    A_TUBE: float = 0.0
     GAMMA: float = GAMMA_DEFAULT
     SFF: float = f32(0.8)   # 3dmhdparam.h:111
     z_stretch: float = 1.5  # tanh stretch factor; 0 gives the reference's uniform grid

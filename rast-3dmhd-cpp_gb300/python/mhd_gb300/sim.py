@@ -52,6 +52,7 @@ def static_state(case: Case, nPEy: int | None = None, nPEz: int | None = None) -
     sp = abi.MhdStaticParams()
     sp.nPEy = case.nPEy if nPEy is None else nPEy
     sp.nPEz = case.nPEz if nPEz is None else nPEz
+    sp.nTube = case.nTube
     for k in ("zMax", "PZP", "SIGMA", "POLYS", "AMPT", "AMPB", "BFH", "BZP"):
         setattr(sp, k, float(getattr(case, k)))
     zee = np.ascontiguousarray(coordinates(case)[2], dtype=np.float64)

@@ -93,8 +93,26 @@ def test_static_rejects_what_is_not_built():
     sp.nPEz = 3  # nPz = 8 does not split over 3 z ranks
     assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_INVALID
     sp.nPEz = 2
+    sp.nTube = 4  # tube models give the reference no state
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_UNSUPPORTED
+    sp.nTube = 6
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_INVALID
+    sp.nTube = 0
     sp.ZEE = None
     assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_INVALID
+
+
+def test_reference_tube_model_aborts():
+    """tube() with nTube = 1 (a twisted Gaussian tube) integrates its pressure
+    balance with qromb, whose polint divides by ho - hp = 0 on its first pass
+    (3dmhdphsic.h:199-208), so the reference aborts: there is no state to match."""
+    refcase = pytest.importorskip("refcase")
+    if not refcase.reference_available():
+        pytest.skip("reference sources not present")
+    case = _case("static_layer").replace(AMPB=0.0, AMPT=0.0, nTube=1, XCENT=3.0, ZCENT=1.0, R_MAX=0.5,
+                                         C_MT=0.1, A_TUBE=0.3, name="static_tube1")
+    with pytest.raises(RuntimeError, match="Failure in polint"):
+        refcase.run(case, {k: np.zeros(case.shape) for k in STATE_FIELDS}, "static", 0, timeout=300)
 
 
 def test_static_live_reference_other_rank_grid():
