@@ -666,6 +666,8 @@ int mhd_destroy(mhd_ctx* ctx) {
     for (cudaEvent_t e : ctx->slab_events) cudaEventDestroy(e);
     if (ctx->s_up) cudaStreamDestroy(ctx->s_up);
     if (ctx->s_down) cudaStreamDestroy(ctx->s_down);
+    for (cudaStream_t st : ctx->s_sub)
+        if (st) cudaStreamDestroy(st);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MHD_OK;

@@ -57,8 +57,10 @@ struct mhd_ctx {
     double pl_TP = 0.0, pl_TC = 0.0, pl_QFH = 0.0, pl_OCV = 0.0;
     double* d_plume = nullptr;  // plx (nx), ply (ny), plz (nz)
     double* d_lrem = nullptr;   // lRem: TTM, HRAD, G (3 x nz)
-    // host-to-host steps: copy streams and per-slab events (created on first use)
+    // host-to-host steps: copy streams, one compute stream per RK3 substage and
+    // per-slab events (created on first use)
     cudaStream_t s_up = nullptr, s_down = nullptr;
+    cudaStream_t s_sub[3] = {nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> slab_events;
 };
 

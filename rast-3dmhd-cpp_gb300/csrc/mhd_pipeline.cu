@@ -3,18 +3,23 @@
 //
 // A driver that keeps its state in host memory (the reference's arrays) pays
 // an upload and a download of the whole state around every step.  Here the
-// interior z planes are cut into slabs and the step runs as a wavefront over
-// three streams:
-//   copy-in stream   slab j (all fields) -> U[cur], then event up[j]
-//   compute stream   S1(t) after up[t+1];  S2(t-1);  S3(t-2), then event done[t-2]
-//   copy-out stream  slab j of the new state after done[j]
+// interior z planes are cut into slabs and the step runs as a dataflow over
+// five streams, one per kind of work:
+//   copy-in          slab j (all fields) -> U[cur], then event up[j]
+//   substage s=1..3  S_s(j) after the event of slab j+1 one stage before
+//                    (up[j+1] for S1, S1 done[j+1] for S2, S2 done[j+1] for S3)
+//   copy-out         slab j of the new state after S3 done[j]
 // Substage s of slab j reads its neighbours one plane beyond the slab, which
-// substage s-1 has finished by then (slab j+1 was issued earlier on the same
-// stream); the wall BCON of each substage follows the first / last slab.  The
-// in-place reads and writes of the ping-pong buffers are ordered by the issue
-// order: S1(j+1) is issued before S2(j) overwrites the plane it reads, and
-// S2(j+1) before S3(j).  Every cell goes through the same arithmetic as in
-// mhd_step, so the result is bit-identical to upload + mhd_step + download.
+// stage s-1 of slab j+1 has produced by then; the same event orders the
+// in-place ping-pong writes (S2(j) overwrites U[cur] planes that S1 of slabs
+// j-1..j+1 read, S3(j) overwrites U[1-cur] planes that S2 of slabs j-1..j+1
+// read), and the substages of one slab follow one another through it.  The
+// wall BCON of each substage follows its first / last slab on the same
+// stream.  Kernels of different substages run concurrently, so one kernel's
+// last wave overlaps the next kernel's first instead of draining the GPU; the
+// later substages have the higher stream priority, so the pipeline drains
+// early.  Every cell goes through the same arithmetic as in mhd_step, so the
+// result is bit-identical to upload + mhd_step + download.
 #include "mhd_context.h"
 
 #include <algorithm>
@@ -84,28 +89,41 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
     if (!rc) rc = ctxops::plume_update(ctx, ctx->timt);
     if (rc) return rc;
     if (!ctx->s_up) {
+        int lo = 0, hi = 0;
+        PCK(cudaDeviceGetStreamPriorityRange(&lo, &hi));  // hi: numerically smallest, most urgent
         PCK(cudaStreamCreateWithFlags(&ctx->s_up, cudaStreamNonBlocking));
         PCK(cudaStreamCreateWithFlags(&ctx->s_down, cudaStreamNonBlocking));
+        for (int s = 0; s < 3; s++) {
+            const int pr = lo + (hi - lo) * s / 2;  // S1 least urgent, S3 most
+            PCK(cudaStreamCreateWithPriority(&ctx->s_sub[s], cudaStreamNonBlocking, pr));
+        }
     }
-    const size_t need = 2 * (size_t)ns + 2;
+    const size_t need = 4 * (size_t)ns + 2;
     while (ctx->slab_events.size() < need) {
         cudaEvent_t e;
         PCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ctx->slab_events.push_back(e);
     }
-    cudaEvent_t* up = ctx->slab_events.data();          // [ns]
-    cudaEvent_t* done = up + ns;                        // [ns]
-    cudaEvent_t start = done[ns], fin = done[ns + 1];
+    // ev[0] = up[ns], ev[1..3] = done of substage 1..3 [ns]
+    cudaEvent_t* ev[4] = {ctx->slab_events.data(), ctx->slab_events.data() + ns, ctx->slab_events.data() + 2 * ns,
+                          ctx->slab_events.data() + 3 * ns};
+    cudaEvent_t start = ctx->slab_events[4 * (size_t)ns], fin = ctx->slab_events[4 * (size_t)ns + 1];
     auto lo_of = [&](int j) { return j == 0 ? 0 : b[j]; };       // with the ghost planes
     auto hi_of = [&](int j) { return j == ns - 1 ? nz : b[j + 1]; };
 
     const int cur = ctx->cur;
     double* Uin = ctx->U[cur];
     double* Uout = ctx->U[1 - cur];  // after three substages the state is in U[1-cur]
-    // the copy streams start after everything queued on the context's stream
+    if (!in) {
+        int r2 = ctxops::sync_zghosts(ctx);
+        if (r2) return r2;
+    }
+    ctx->ghosts_synced = true;
+    // every stream starts after everything queued on the context's stream
     PCK(cudaEventRecord(start, ctx->stream));
     PCK(cudaStreamWaitEvent(ctx->s_up, start, 0));
     PCK(cudaStreamWaitEvent(ctx->s_down, start, 0));
+    for (int s = 0; s < 3; s++) PCK(cudaStreamWaitEvent(ctx->s_sub[s], start, 0));
     for (int j = 0; j < ns; j++) {
         if (in) {
             PCK(copy_planes(ctx, Uin, const_cast<double*>(in), lo_of(j), hi_of(j), true, ctx->s_up));
@@ -113,43 +131,39 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
             if (j == 0) PCK(copy_planes(ctx, Uout, const_cast<double*>(in), 0, 1, true, ctx->s_up));
             if (j == ns - 1) PCK(copy_planes(ctx, Uout, const_cast<double*>(in), nz - 1, nz, true, ctx->s_up));
         }
-        PCK(cudaEventRecord(up[j], ctx->s_up));
+        PCK(cudaEventRecord(ev[0][j], ctx->s_up));
     }
-    if (!in) {
-        int r2 = ctxops::sync_zghosts(ctx);
-        if (r2) return r2;
-    }
-    ctx->ghosts_synced = true;
 
     auto substage = [&](int s, int j) -> int {
+        cudaStream_t st = ctx->s_sub[s];
         FusedArgs a = ctxops::fused_args(ctx, s, dt, s == 1 ? 1 - cur : cur);
         a.zlo = b[j];
         a.zhi = b[j + 1];
-        int e = fused_substage(ctx->sw, a, ctx->stream);
+        int e = fused_substage(ctx->sw, a, st);
         if (e) return fail_cuda(ctx, (cudaError_t)e, "fused substage launch");
-        if (j == 0) e = fused_bcon_wall(ctx->sw, ctx->g, ctx->c, a.Uo, ctx->timt, 0, ctx->stream);
-        if (!e && j == ns - 1) e = fused_bcon_wall(ctx->sw, ctx->g, ctx->c, a.Uo, ctx->timt, 1, ctx->stream);
+        if (j == 0) e = fused_bcon_wall(ctx->sw, ctx->g, ctx->c, a.Uo, ctx->timt, 0, st);
+        if (!e && j == ns - 1) e = fused_bcon_wall(ctx->sw, ctx->g, ctx->c, a.Uo, ctx->timt, 1, st);
         if (e) return fail_cuda(ctx, (cudaError_t)e, "BCON launch");
         return MHD_OK;
     };
+    // issue in wavefront order (S1 of slab t, S2 of t-1, S3 of t-2), so each
+    // wait names an event that is already recorded
     for (int t = 0; t < ns + 2; t++) {
-        if (t < ns) {
-            PCK(cudaStreamWaitEvent(ctx->stream, up[std::min(t + 1, ns - 1)], 0));
-            if ((rc = substage(0, t))) return rc;
-        }
-        if (t - 1 >= 0 && t - 1 < ns && (rc = substage(1, t - 1))) return rc;
-        if (t - 2 >= 0 && t - 2 < ns) {
-            const int j = t - 2;
-            if ((rc = substage(2, j))) return rc;
-            PCK(cudaEventRecord(done[j], ctx->stream));
-            if (out) {
-                PCK(cudaStreamWaitEvent(ctx->s_down, done[j], 0));
+        for (int s = 0; s < 3; s++) {
+            const int j = t - s;
+            if (j < 0 || j >= ns) continue;
+            PCK(cudaStreamWaitEvent(ctx->s_sub[s], ev[s][std::min(j + 1, ns - 1)], 0));
+            if ((rc = substage(s, j))) return rc;
+            PCK(cudaEventRecord(ev[s + 1][j], ctx->s_sub[s]));
+            if (s == 2 && out) {
+                PCK(cudaStreamWaitEvent(ctx->s_down, ev[3][j], 0));
                 PCK(copy_planes(ctx, Uout, out, lo_of(j), hi_of(j), false, ctx->s_down));
             }
         }
     }
-    // later work on the context's stream waits for the copies
-    PCK(cudaEventRecord(fin, ctx->s_down));
+    // later work on the context's stream waits for the last download (or the
+    // last S3 kernel), which follow every other operation of the step
+    PCK(cudaEventRecord(fin, out ? ctx->s_down : ctx->s_sub[2]));
     PCK(cudaStreamWaitEvent(ctx->stream, fin, 0));
     ctx->cur = 1 - cur;
     ctxops::advance_time(ctx, dt);
