@@ -331,7 +331,7 @@ def run_ours(args, dist: Dist) -> None:
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps if e2e_steps else None,
                 "path": "mhd_step_host: pinned host state in and out, upload / 3 substages / download "
-                        "overlapped over z slabs on three streams",
+                        "overlapped over z slabs (uploads, one stream per substage, downloads)",
                 "serial_transfers": {"value": dist.world * case.cells / serial_s if e2e_steps else None,
                                      "ms_per_step": 1e3 * serial_s if e2e_steps else None,
                                      "path": "mhd_upload_state + mhd_step + mhd_download_state"}},

@@ -245,7 +245,8 @@ int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out);
  * doubles, field-major as in mhd_upload_state; they may be the same buffer;
  * pinned memory (mhd_host_alloc) lets the copies overlap the computation).
  * The interior is cut into z slabs that are uploaded, stepped and downloaded
- * as a wavefront on three streams, so the copies hide behind the kernels;
+ * as a dataflow over five streams (uploads, one per RK3 substage, downloads),
+ * so the copies hide behind the kernels;
  * the result is bit-identical to mhd_upload_state + mhd_step +
  * mhd_download_state.  in = NULL steps the device state; out = NULL skips the
  * download and the call does not block (then `in` must stay unchanged until
