@@ -501,6 +501,24 @@ __device__ __forceinline__ double cfl_a1(const Consts& c, double DD, double ro, 
 __device__ __forceinline__ double cfl_a2(const Consts& c, double DD, double ro) { return 0.375f * DD * DD * c.RE * ro; }
 __device__ __forceinline__ double cfl_a3(const Consts& c, double DD) { return 0.5f * DD * DD * c.RM; }
 
+// float value of d with its significand truncated to 23 bits (relative error
+// below 2^-23), formed with integer operations only; magnitudes below 2^-126
+// become 0 and magnitudes beyond the float range (and NaN) become infinity.
+__device__ __forceinline__ float trunc_to_f32(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);
+    unsigned b;
+    if (e <= 0) b = sign;
+    else if (e >= 255) b = sign | 0x7f800000u;
+    else b = sign | ((unsigned)e << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
+    return __uint_as_float(b);
+}
+
+__device__ __forceinline__ bool nonzero_bits(double d) {
+    return (((unsigned)__double2hiint(d) & 0x7fffffffu) | (unsigned)__double2loint(d)) != 0u;
+}
+
 // Field access of the CFL reduction: FP64 state, or FP32-storage state
 // (deviations from the FP64 profiles rho0(z), T0(z)) widened to FP64.
 struct CflFields64 {
@@ -508,6 +526,9 @@ struct CflFields64 {
     __device__ double f(int k, long long i) const { return U.p[k][i]; }
     __device__ double ro(long long i, int) const { return U.p[S_RO][i]; }
     __device__ double tt(long long i, int) const { return U.p[S_TT][i]; }
+    // the estimate's float input of field k (truncated to 23 bits) and whether it is nonzero
+    __device__ float fe(int k, long long i) const { return trunc_to_f32(U.p[k][i]); }
+    __device__ bool nz(int k, long long i) const { return nonzero_bits(U.p[k][i]); }
 };
 struct CflFields32 {
     Fields8f U;
@@ -515,6 +536,9 @@ struct CflFields32 {
     __device__ double f(int k, long long i) const { return widen_f32(U.p[k][i]); }
     __device__ double ro(long long i, int z) const { return bgR[z] + widen_f32(U.p[S_RO][i]); }
     __device__ double tt(long long i, int z) const { return bgT[z] + widen_f32(U.p[S_TT][i]); }
+    // stored floats are their own estimate input (exact; subnormals kept)
+    __device__ float fe(int k, long long i) const { return U.p[k][i]; }
+    __device__ bool nz(int k, long long i) const { return (__float_as_uint(U.p[k][i]) & 0x7fffffffu) != 0u; }
 };
 
 // mc and the fast-mode speed^2 UU' of cell i (plane z)
@@ -582,39 +606,21 @@ __device__ void write_cfl_partials(double um, double w0, double w1, double w2, d
         for (int k = 0; k < 5; k++) part[(long long)k * gridDim.x + blockIdx.x] = s[k][0];
 }
 
-// float value of d with its significand truncated to 23 bits (relative error
-// below 2^-23), formed with integer operations only; magnitudes below 2^-126
-// become 0 and magnitudes beyond the float range (and NaN) become infinity.
-__device__ __forceinline__ float trunc_to_f32(double d) {
-    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    const unsigned sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);
-    unsigned b;
-    if (e <= 0) b = sign;
-    else if (e >= 255) b = sign | 0x7f800000u;
-    else b = sign | ((unsigned)e << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
-    return __uint_as_float(b);
-}
-
-__device__ __forceinline__ bool nonzero_bits(double d) {
-    return (((unsigned)__double2hiint(d) & 0x7fffffffu) | (unsigned)__double2loint(d)) != 0u;
-}
 
 // FP32 estimates of cell i's fast-mode candidate a0 and of mc (both certified
 // to 1.2e-6 when `ok`), and whether its momenta are not all exactly zero.
 template <bool MAG, class FA>
 __device__ __forceinline__ void cfl_estimate(const FA& U, long long i, int z, float ddf, float gam_f, float obeta_f,
                                              double rod, float& a0, float& mc, bool& ok, bool& nz) {
-    const double rud = U.f(S_RU, i), rvd = U.f(S_RV, i), rwd = U.f(S_RW, i), ttd = U.tt(i, z);
-    nz = nonzero_bits(rud) || nonzero_bits(rvd) || nonzero_bits(rwd);
-    const float ru = trunc_to_f32(rud), rv = trunc_to_f32(rvd), rw = trunc_to_f32(rwd);
-    const float ro = trunc_to_f32(rod), tt = trunc_to_f32(ttd);
+    const float ru = U.fe(S_RU, i), rv = U.fe(S_RV, i), rw = U.fe(S_RW, i);
+    nz = U.nz(S_RU, i) | U.nz(S_RV, i) | U.nz(S_RW, i);  // no short circuit: the loads stay unconditional
+    const float ro = trunc_to_f32(rod), tt = trunc_to_f32(U.tt(i, z));
     const float ir = __frcp_rn(ro);
     const float sq = __fadd_rn(__fadd_rn(__fmul_rn(ru, ru), __fmul_rn(rv, rv)), __fmul_rn(rw, rw));
     const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
     float G = __fmul_rn(gam_f, tt);
     if constexpr (MAG) {
-        const float bx = trunc_to_f32(U.f(S_BX, i)), by = trunc_to_f32(U.f(S_BY, i)), bz = trunc_to_f32(U.f(S_BZ, i));
+        const float bx = U.fe(S_BX, i), by = U.fe(S_BY, i), bz = U.fe(S_BZ, i);
         const float b2 = __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
         G = __fadd_rn(G, __fmul_rn(__fmul_rn(obeta_f, b2), ir));
     }
@@ -654,7 +660,8 @@ __global__ void k_cfl_seed(Grid g, Consts c, FA U, unsigned* seed) {
         if (!cfl_fast_row(g, c, y, z, DDyz)) continue;
         const float ddf = narrow_f64(DDyz);
         const long long row = (long long)z * g.sz + (long long)y * g.sy;
-        for (int x = 1 + lane; x <= nPx; x += 32) {
+#pragma unroll 4
+        for (int x = 1 + lane; x <= nPx; x += 32) {  // unrolled: the cells' loads overlap
             float a0, mc;
             bool ok, nz;
             cfl_estimate<MAG>(U, row + x, z, ddf, gam_f, obeta_f, U.ro(row + x, z), a0, mc, ok, nz);
@@ -689,7 +696,8 @@ constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x t
 //     depends on DD alone; rounding is monotone, so their row minima are the
 //     candidates of the row's smallest ro (an exact FP64 min);
 //   * mc and a0 = DD/sqrt(UU') are estimated in FP32 from inputs truncated to
-//     23 bits (error below 1.2e-6 for inputs in the accepted ranges); a cell is
+//     23 bits, or read as stored with FP32 storage (error below 1.2e-6 for
+//     inputs in the accepted ranges); a cell is
 //     evaluated exactly when its estimate lies within 2^-16 of the best
 //     estimate the warp has seen so far (the running maximum of mc, minimum of
 //     a0, the current pass included), or when its estimate is not certified
