@@ -235,3 +235,42 @@ def test_cfl_reduction_after_fused_steps():
     sim.close()
     want = oracle.OracleSim(case, st).cfl_dt()
     assert got == want
+
+
+@pytest.mark.parametrize("kind", ["run", "ties", "tiny_and_odd"])
+def test_fp32_cfl_reduction_bit_exact(kind):
+    """FP32 storage: the filtered reduction reads the stored floats as its
+    estimates and reduces the widened FP64 state (profile + deviation) exactly;
+    DT and UMACH equal the oracle's cell-by-cell reduction over the state
+    mhd_download_state returns (the same FP64 values), bit for bit, for an
+    evolved flow, a state of ties, and tiny, subnormal-float, huge and
+    negative values."""
+    case = Case(nPx=70, nPy=36, nPz=20, lMag=True, lRot=True, seed=12, noise=1e-2, name="cfl32x")
+    sim = Simulation(case, precision="fp32")
+    if kind == "run":
+        sim.upload_state(initial_state(case))
+        sim.communicate()
+        sim.steps_cfl(10)
+    else:
+        if kind == "ties":
+            st = initial_state(case)
+            st["TT"][...] = 2.0
+            st["RO"][...] = 0.5
+            st["RU"][...] = 0.01
+            st["RV"][...] = -0.02
+            st["RW"][...] = 0.0
+        else:
+            st = _random_flow(case, 5, 1e-25)
+            st["RU"][7, 9, 11] = 3e-3                  # one real flow cell
+            st["RV"][4, 10, 20] = 1e-41                # a subnormal float once stored
+            st["BX"][5, 5, 5] = 3e-44                  # subnormal field value
+            st["RV"][5, 20, 40] = 1e30                 # huge momentum
+            st["TT"][9, 3, 3] = -0.5                   # negative temperature
+        sim.upload_state(st)
+        sim.communicate()
+    state = sim.download_state()
+    got = sim.cfl_dt()
+    sim.close()
+    want = oracle.OracleSim(case, state).cfl_dt()
+    assert got[0] == want[0] or (np.isnan(got[0]) and np.isnan(want[0])), (got, want)
+    assert got[1] == want[1] or (np.isnan(got[1]) and np.isnan(want[1])), (got, want)
