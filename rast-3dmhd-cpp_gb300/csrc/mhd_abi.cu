@@ -553,6 +553,30 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     bool uxy = true;
     for (int i = 0; i < nx; i++) uxy = uxy && p.d2xxdx2[i] == 0.0;
     for (int i = 0; i < ny; i++) uxy = uxy && p.d2yydy2[i] == 0.0;
+    // ... and the same first-derivative and 'b' coefficients in every interior column
+    auto same = [&](size_t off, int n) {
+        bool eq = true;
+        for (int i = 2; i <= n - 2; i++) eq = eq && h[off + i] == h[off + 1];
+        return eq;
+    };
+    for (int ax = 0; ax < 2 && uxy; ax++) {
+        uxy = same(base_off[ax], ns[ax]) && same(base_off[ax] + 2 * (size_t)ns[ax], ns[ax]);
+        for (int k = 1; k < 6 && uxy; k += 2) uxy = same(scaled_off[ax] + (size_t)k * ns[ax], ns[ax]);
+    }
+    // per-z sums of the Laplacians' 'b' coefficients (used with uniform x / y grids)
+    const size_t lap_off = h.size();
+    {
+        auto sb = [&](int ax, int k, int i) { return h[scaled_off[ax] + (size_t)(2 * k + 1) * ns[ax] + i]; };
+        auto pb = [&](int ax, int i) { return h[base_off[ax] + 2 * (size_t)ns[ax] + i]; };
+        const int kx[6] = {1, 0, 0, -1, 2, 2}, ky[6] = {0, 1, 0, -1, 2, 2}, kz[6] = {0, 0, 1, -1, 2, -2};
+        for (int set = 0; set < 6; set++)
+            for (int z = 0; z < nz; z++) {
+                const double sx = kx[set] < 0 ? pb(0, 1) : sb(0, kx[set], 1);
+                const double sy = ky[set] < 0 ? pb(1, 1) : sb(1, ky[set], 1);
+                const double sz = kz[set] == -2 ? 0.0 : kz[set] < 0 ? pb(2, z) : sb(2, kz[set], z);
+                h.push_back(2.0 * (sx + sy + sz));
+            }
+    }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
@@ -579,6 +603,7 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         ctx->coef.kapz = b0 + kap_off;
         ctx->coef.dkapz = b0 + kap_off + nz;
         ctx->coef.uniform_xy = uxy ? 1 : 0;
+        for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lap_off + (size_t)set * nz;
     }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;

@@ -80,7 +80,14 @@ struct Coefs {
     // folded in, per axis: ORE*c2a, ORE*c2b, ORE*C43*c2a, ORE*C43*c2b, ORM*c2a, ORM*c2b
     const double* s2[3][6];
     const double *kapz, *dkapz;  // (OCV/REPR)*RKAPA[z], (OCV/REPR)*DKAPA[z]
-    int uniform_xy;              // d2xxdx2 and d2yydy2 vanish everywhere
+    // uniform x and y grids: d2xxdx2 and d2yydy2 vanish and the x / y
+    // coefficients are the same in every interior column
+    int uniform_xy;
+    // with uniform_xy, per z: S = 2 (sx + sy + sz) of the second-derivative
+    // coefficients (the 'b' ones) of the Laplacians of u, v, w (viscous,
+    // C43 on the x, y, z axis respectively), T (plain), B (resistive), and
+    // 2 (sx + sy) of B for the wall planes
+    const double* lapS[6];
 };
 
 // ---- launchers implemented in the .cu files ----------------------------

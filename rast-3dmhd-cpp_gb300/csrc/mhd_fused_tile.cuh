@@ -20,8 +20,11 @@
 //     c2b = duudu^2*h2u), and the viscous (ORE, ORE*C43) and resistive (ORM)
 //     scales are folded into copies of c2a/c2b, so a scaled second derivative
 //     accumulates with three FMAs (five where d2uudu2 does not vanish);
-//   * UXY (uniform x and y grids, d2uudu2 = 0) drops the first-derivative
-//     part of the x/y second derivatives at compile time;
+//   * UXY (uniform x and y grids: d2uudu2 = 0, the same coefficients in
+//     every column) drops the first-derivative part of the x/y second
+//     derivatives at compile time and sums each Laplacian as
+//     sx (px + mx) + sy (py + my) + sz (pz + mz) - c S with S = 2 (sx + sy + sz)
+//     from a per-z table: one -2c product instead of one per axis;
 //   * repeated gradients are computed once; 1/rho is Newton's iteration
 //     r <- r + r(1 - rho r), twice, from the hardware reciprocal estimate.
 // Results agree with the reference to rounding (1e-12 of each field's
@@ -194,6 +197,15 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             auto lapx = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, XP(q), XM(q), C0(q), sx[2 * k], sx[2 * k + 1]); };
             auto lapy = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, YP(q), YM(q), C0(q), sy[2 * k], sy[2 * k + 1]); };
             auto lapz = [&](double acc, int q, int k) { return acc_d2<true>(acc, ZP(q), ZM(q), C0(q), sz[2 * k], sz[2 * k + 1]); };
+            // uniform x / y: acc + sxb (px + mx) + syb (py + my) + (sza (pz - mz) + szb (pz + mz)) - c S,
+            // S = 2 (sxb + syb + szb) from the per-z table: one -2c product for the three axes
+            auto lap3 = [&](double acc, int q, double sxb, double syb, double sza, double szb, double S) {
+                acc = fma(ZP(q) - ZM(q), sza, acc);
+                acc = fma(XP(q) + XM(q), sxb, acc);
+                acc = fma(YP(q) + YM(q), syb, acc);
+                acc = fma(ZP(q) + ZM(q), szb, acc);
+                return fma(-C0(q), S, acc);
+            };
 
             const double ro = C0(Q_RO), ri = C0(Q_RI), tt = C0(Q_TT);
             const double u = C0(Q_U), v = C0(Q_V), w = C0(Q_W);
@@ -230,9 +242,14 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 ft = a.FT[i];  // the reference never re-initialises FT with lShr
             }
             {
-                double lapT = acc_d2<!UXY>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
-                lapT = acc_d2<!UXY>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
-                lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
+                double lapT;
+                if constexpr (UXY) {
+                    lapT = lap3(0.0, Q_TT, cx2b, cy2b, cz2a, cz2b, K.lapS[3][z]);
+                } else {
+                    lapT = acc_d2<true>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
+                    lapT = acc_d2<true>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
+                    lapT = acc_d2<true>(lapT, ZP(Q_TT), ZM(Q_TT), C0(Q_TT), cz2a, cz2b);
+                }
                 if (EXTRA && c.lrem && !SW::lShr) {
                     // lRem: conduction of T - TTM(z) plus HRAD (3dmhdsub.h:297-313),
                     // as lap T + (HRAD - d2 TTM/dz2), the latter precomputed per z
@@ -246,10 +263,16 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
             }
 
-            // ---- viscous Laplacians (3dmhdsub.h:462-472)
-            fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
-            fv = lapz(lapy(lapx(fv, Q_V, 0), Q_V, 1), Q_V, 0);
-            fw = lapz(lapy(lapx(fw, Q_W, 0), Q_W, 0), Q_W, 1);
+            // ---- viscous Laplacians (3dmhdsub.h:462-472); scale pairs sx[2k], sx[2k+1]
+            if constexpr (UXY) {
+                fu = lap3(fu, Q_U, sx[3], sy[1], sz[0], sz[1], K.lapS[0][z]);
+                fv = lap3(fv, Q_V, sx[1], sy[3], sz[0], sz[1], K.lapS[1][z]);
+                fw = lap3(fw, Q_W, sx[1], sy[1], sz[2], sz[3], K.lapS[2][z]);
+            } else {
+                fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
+                fv = lapz(lapy(lapx(fv, Q_V, 0), Q_V, 1), Q_V, 0);
+                fw = lapz(lapy(lapx(fw, Q_W, 0), Q_W, 0), Q_W, 1);
+            }
 
             // ---- viscous cross terms (3dmhdsub.h:486-487,517-518,531-532)
             {
@@ -315,15 +338,32 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 const double bzx = Dx(Q_BZ), bzy = Dy(Q_BZ), bzz = Dz(Q_BZ);
                 w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
                 w1 = fma(-u, bxx, fma(-v, bxy, fma(-w, bxz, w1)));
-                w1 = lapy(lapx(w1, Q_BX, 2), Q_BX, 2);
                 w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
                 w2 = fma(-u, byx, fma(-v, byy, fma(-w, byz, w2)));
-                w2 = lapy(lapx(w2, Q_BY, 2), Q_BY, 2);
                 w3 = fma(bx, wx, fma(by, wy, -bz * (ux + vy)));
                 w3 = fma(-u, bzx, fma(-v, bzy, fma(-w, bzz, w3)));
-                w3 = lapz(lapy(lapx(w3, Q_BZ, 2), Q_BZ, 2), Q_BZ, 2);
+                const bool wall = (z == zl || z == zr - 1);
+                if constexpr (UXY) {
+                    w3 = lap3(w3, Q_BZ, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
+                    if (wall) {
+                        // x and y parts only: acc + sxb (px + mx) + syb (py + my) - c 2 (sxb + syb)
+                        w1 = fma(-bx, K.lapS[5][z], fma(YP(Q_BX) + YM(Q_BX), sy[5], fma(XP(Q_BX) + XM(Q_BX), sx[5], w1)));
+                        w2 = fma(-by, K.lapS[5][z], fma(YP(Q_BY) + YM(Q_BY), sy[5], fma(XP(Q_BY) + XM(Q_BY), sx[5], w2)));
+                    } else {
+                        w1 = lap3(w1, Q_BX, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
+                        w2 = lap3(w2, Q_BY, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
+                    }
+                } else {
+                    w1 = lapy(lapx(w1, Q_BX, 2), Q_BX, 2);
+                    w2 = lapy(lapx(w2, Q_BY, 2), Q_BY, 2);
+                    w3 = lapz(lapy(lapx(w3, Q_BZ, 2), Q_BZ, 2), Q_BZ, 2);
+                    if (!wall) {
+                        w1 = lapz(w1, Q_BX, 2);
+                        w2 = lapz(w2, Q_BY, 2);
+                    }
+                }
                 // d2B/dz2 with the one-sided wall stencils (3dmhdsub.h:640-654,673-687)
-                if (z == zl || z == zr - 1) {
+                if (wall) {
                     const int s = (z == zl) ? 1 : -1;
                     const long long j2 = i + 2 * s * g.sz, j3 = i + 3 * s * g.sz;
                     const double d2 = c.d2zzdz2[z] * c.hz * c.ORM, d1 = c.dzzdz[z] * c.dzzdz[z] * c.h2z * c.ORM;
@@ -332,9 +372,6 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     const double sg = (double)s;
                     w1 += sg * (-3.0 * bx + 4.0 * X1 - X2) * d2 + (2.0 * bx - 5.0 * X1 + 4.0 * X2 - X3) * d1;
                     w2 += sg * (-3.0 * by + 4.0 * Y1 - Y2) * d2 + (2.0 * by - 5.0 * Y1 + 4.0 * Y2 - Y3) * d1;
-                } else {
-                    w1 = lapz(w1, Q_BX, 2);
-                    w2 = lapz(w2, Q_BY, 2);
                 }
                 const double jz = byx - bxy, jy = bxz - bzx, jx = bzy - byz;
                 fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
