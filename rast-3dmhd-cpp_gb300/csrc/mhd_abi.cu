@@ -576,6 +576,11 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
                 const double sz = kz[set] == -2 ? 0.0 : kz[set] < 0 ? pb(2, z) : sb(2, kz[set], z);
                 h.push_back(2.0 * (sx + sy + sz));
             }
+        // the kernel's C13*ORE*cx1*cz1 and C13*ORE*cy1*cz1, same order of operations
+        const double c13ore = ctx->k.C13 * ctx->k.ORE;
+        const double kx13 = c13ore * h[base_off[0] + 1], ky13 = c13ore * h[base_off[1] + 1];
+        for (int z = 0; z < nz; z++) h.push_back(kx13 * h[base_off[2] + z]);
+        for (int z = 0; z < nz; z++) h.push_back(ky13 * h[base_off[2] + z]);
     }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -604,6 +609,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         ctx->coef.dkapz = b0 + kap_off + nz;
         ctx->coef.uniform_xy = uxy ? 1 : 0;
         for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lap_off + (size_t)set * nz;
+        ctx->coef.kxz = b0 + lap_off + 6 * (size_t)nz;
+        ctx->coef.kyz = b0 + lap_off + 7 * (size_t)nz;
     }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;

@@ -88,6 +88,8 @@ struct Coefs {
     // C43 on the x, y, z axis respectively), T (plain), B (resistive), and
     // 2 (sx + sy) of B for the wall planes
     const double* lapS[6];
+    // with uniform_xy, per z: the viscous cross-term factors C13*ORE*cx1*cz1 and C13*ORE*cy1*cz1
+    const double *kxz, *kyz;
 };
 
 // ---- launchers implemented in the .cu files ----------------------------

@@ -276,7 +276,14 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
 
             // ---- viscous cross terms (3dmhdsub.h:486-487,517-518,531-532)
             {
-                const double kxz = kx13 * cz1, kyz = ky13 * cz1;
+                double kxz, kyz;
+                if constexpr (UXY) {
+                    kxz = K.kxz[z];
+                    kyz = K.kyz[z];
+                } else {
+                    kxz = kx13 * cz1;
+                    kyz = ky13 * cz1;
+                }
                 auto E = [&](const double* Pl, int q, int off) { return Pl[q * kPlane + pc + off]; };
                 const double dyxv = (E(P0, Q_V, kPX + 1) - E(P0, Q_V, kPX - 1)) - (E(P0, Q_V, -kPX + 1) - E(P0, Q_V, -kPX - 1));
                 const double dyxu = (E(P0, Q_U, kPX + 1) - E(P0, Q_U, kPX - 1)) - (E(P0, Q_U, -kPX + 1) - E(P0, Q_U, -kPX - 1));
@@ -289,9 +296,9 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 fw = fma(kxz, dxzu, fma(kyz, dyzv, fw));
             }
 
-            // velocity gradients (heating and induction)
+            // velocity gradients (heating and, without lShr, induction)
             double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
-            if constexpr (!SW::lShr || SW::lMag) {
+            if constexpr (!SW::lShr) {
                 ux = Dx(Q_U); uy = Dy(Q_U); uz = Dz(Q_U);
                 vx = Dx(Q_V); vy = Dy(Q_V); vz = Dz(Q_V);
                 wx = Dx(Q_W); wy = Dy(Q_W); wz = Dz(Q_W);
@@ -323,25 +330,61 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             double w1 = 0, w2 = 0, w3 = 0;
             if constexpr (SW::lMag) {
                 const double bx = C0(Q_BX), by = C0(Q_BY), bz = C0(Q_BZ);
-                // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
-                double wzm = wz;
-                if (z == zl) {
-                    const long long j = i + 2 * g.sz;
-                    wzm = (4.0 * ZP(Q_W) - a.U.p[S_RW][j] / a.U.p[S_RO][j]) * cz1;
+                double jx, jy, jz;
+                if constexpr (SW::lShr) {
+                    // the velocity gradients feed the induction terms only: group each
+                    // component's terms by axis over raw differences and apply the axis'
+                    // metric factor once per group
+                    const double dUx = XP(Q_U) - XM(Q_U), dUy = YP(Q_U) - YM(Q_U), dUz = ZP(Q_U) - ZM(Q_U);
+                    const double dVx = XP(Q_V) - XM(Q_V), dVy = YP(Q_V) - YM(Q_V), dVz = ZP(Q_V) - ZM(Q_V);
+                    const double dWx = XP(Q_W) - XM(Q_W), dWy = YP(Q_W) - YM(Q_W);
+                    double dWz = ZP(Q_W) - ZM(Q_W);
+                    // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
+                    if (z == zl) {
+                        const long long j = i + 2 * g.sz;
+                        dWz = 4.0 * ZP(Q_W) - a.U.p[S_RW][j] / a.U.p[S_RO][j];
+                    }
+                    if (z == zr - 1) {
+                        const long long j = i - 2 * g.sz;
+                        dWz = a.U.p[S_RW][j] / a.U.p[S_RO][j] - 4.0 * ZM(Q_W);
+                    }
+                    const double dBXx = XP(Q_BX) - XM(Q_BX), dBXy = YP(Q_BX) - YM(Q_BX), dBXz = ZP(Q_BX) - ZM(Q_BX);
+                    const double dBYx = XP(Q_BY) - XM(Q_BY), dBYy = YP(Q_BY) - YM(Q_BY), dBYz = ZP(Q_BY) - ZM(Q_BY);
+                    const double dBZx = XP(Q_BZ) - XM(Q_BZ), dBZy = YP(Q_BZ) - YM(Q_BZ), dBZz = ZP(Q_BZ) - ZM(Q_BZ);
+                    const double cxu = cx1 * u, cyv = cy1 * v, czw = cz1 * w;
+                    w1 = fma(-cxu, dBXx, fma(cy1, fma(by, dUy, fma(-v, dBXy, -bx * dVy)),
+                                             cz1 * fma(bz, dUz, fma(-w, dBXz, -bx * dWz))));
+                    w2 = fma(cx1, fma(bx, dVx, fma(-u, dBYx, -by * dUx)),
+                             fma(-cyv, dBYy, cz1 * fma(bz, dVz, fma(-w, dBYz, -by * dWz))));
+                    w3 = fma(cx1, fma(bx, dWx, fma(-u, dBZx, -bz * dUx)),
+                             fma(cy1, fma(by, dWy, fma(-v, dBZy, -bz * dVy)), -czw * dBZz));
+                    jz = fma(cx1, dBYx, -cy1 * dBXy);
+                    jy = fma(cz1, dBXz, -cx1 * dBZx);
+                    jx = fma(cy1, dBZy, -cz1 * dBYz);
+                } else {
+                    // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
+                    double wzm = wz;
+                    if (z == zl) {
+                        const long long j = i + 2 * g.sz;
+                        wzm = (4.0 * ZP(Q_W) - a.U.p[S_RW][j] / a.U.p[S_RO][j]) * cz1;
+                    }
+                    if (z == zr - 1) {
+                        const long long j = i - 2 * g.sz;
+                        wzm = (a.U.p[S_RW][j] / a.U.p[S_RO][j] - 4.0 * ZM(Q_W)) * cz1;
+                    }
+                    const double bxx = Dx(Q_BX), bxy = Dy(Q_BX), bxz = Dz(Q_BX);
+                    const double byx = Dx(Q_BY), byy = Dy(Q_BY), byz = Dz(Q_BY);
+                    const double bzx = Dx(Q_BZ), bzy = Dy(Q_BZ), bzz = Dz(Q_BZ);
+                    w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
+                    w1 = fma(-u, bxx, fma(-v, bxy, fma(-w, bxz, w1)));
+                    w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
+                    w2 = fma(-u, byx, fma(-v, byy, fma(-w, byz, w2)));
+                    w3 = fma(bx, wx, fma(by, wy, -bz * (ux + vy)));
+                    w3 = fma(-u, bzx, fma(-v, bzy, fma(-w, bzz, w3)));
+                    jz = byx - bxy;
+                    jy = bxz - bzx;
+                    jx = bzy - byz;
                 }
-                if (z == zr - 1) {
-                    const long long j = i - 2 * g.sz;
-                    wzm = (a.U.p[S_RW][j] / a.U.p[S_RO][j] - 4.0 * ZM(Q_W)) * cz1;
-                }
-                const double bxx = Dx(Q_BX), bxy = Dy(Q_BX), bxz = Dz(Q_BX);
-                const double byx = Dx(Q_BY), byy = Dy(Q_BY), byz = Dz(Q_BY);
-                const double bzx = Dx(Q_BZ), bzy = Dy(Q_BZ), bzz = Dz(Q_BZ);
-                w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
-                w1 = fma(-u, bxx, fma(-v, bxy, fma(-w, bxz, w1)));
-                w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
-                w2 = fma(-u, byx, fma(-v, byy, fma(-w, byz, w2)));
-                w3 = fma(bx, wx, fma(by, wy, -bz * (ux + vy)));
-                w3 = fma(-u, bzx, fma(-v, bzy, fma(-w, bzz, w3)));
                 const bool wall = (z == zl || z == zr - 1);
                 if constexpr (UXY) {
                     w3 = lap3(w3, Q_BZ, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
@@ -373,7 +416,6 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     w1 += sg * (-3.0 * bx + 4.0 * X1 - X2) * d2 + (2.0 * bx - 5.0 * X1 + 4.0 * X2 - X3) * d1;
                     w2 += sg * (-3.0 * by + 4.0 * Y1 - Y2) * d2 + (2.0 * by - 5.0 * Y1 + 4.0 * Y2 - Y3) * d1;
                 }
-                const double jz = byx - bxy, jy = bxz - bzx, jx = bzy - byz;
                 fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
                 fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
                 fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
