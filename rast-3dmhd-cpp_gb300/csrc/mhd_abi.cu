@@ -550,6 +550,7 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     const double tmpc = ctx->k.OCV / ctx->k.REPR;
     for (int i = 0; i < nz; i++) h.push_back(tmpc * p.RKAPA[i]);
     for (int i = 0; i < nz; i++) h.push_back(tmpc * p.DKAPA[i]);
+    for (int i = 0; i < nz; i++) h.push_back(tmpc * p.DKAPA[i] * h[base_off[2] + i]);
     bool uxy = true;
     for (int i = 0; i < nx; i++) uxy = uxy && p.d2xxdx2[i] == 0.0;
     for (int i = 0; i < ny; i++) uxy = uxy && p.d2yydy2[i] == 0.0;
@@ -607,6 +608,7 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         }
         ctx->coef.kapz = b0 + kap_off;
         ctx->coef.dkapz = b0 + kap_off + nz;
+        ctx->coef.dkz = b0 + kap_off + 2 * (size_t)nz;
         ctx->coef.uniform_xy = uxy ? 1 : 0;
         for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lap_off + (size_t)set * nz;
         ctx->coef.kxz = b0 + lap_off + 6 * (size_t)nz;

@@ -80,6 +80,7 @@ struct Coefs {
     // folded in, per axis: ORE*c2a, ORE*c2b, ORE*C43*c2a, ORE*C43*c2b, ORM*c2a, ORM*c2b
     const double* s2[3][6];
     const double *kapz, *dkapz;  // (OCV/REPR)*RKAPA[z], (OCV/REPR)*DKAPA[z]
+    const double* dkz;           // dkapz[z] * cz1[z]
     // uniform x and y grids: d2xxdx2 and d2yydy2 vanish and the x / y
     // coefficients are the same in every interior column
     int uniform_xy;

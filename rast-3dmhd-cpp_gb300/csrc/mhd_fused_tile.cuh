@@ -217,24 +217,22 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             if (z == zr - 1) rwz = a.U.p[S_RW][i - 2 * g.sz] - 4.0 * ZM(Q_RW);
             const double fr = -fma(rwz, cz1, fma(YP(Q_RV) - YM(Q_RV), cy1, (XP(Q_RU) - XM(Q_RU)) * cx1));
 
-            // ---- pressure and gravity (3dmhdsub.h:266-272)
-            double fu = -Dx(Q_P);
-            double fv = -Dy(Q_P);
-            double fw = fma(ro, c.GRAV, -Dz(Q_P));
-
-            // ---- momentum advection (3dmhdsub.h:279-289): -D_j(RU_i u_j)
-            fu = fma(-cx1, fma(XP(Q_RU), XP(Q_U), -XM(Q_RU) * XM(Q_U)), fu);
+            // ---- pressure, gravity (3dmhdsub.h:266-272) and momentum advection
+            // (3dmhdsub.h:279-289): F_i = -D_i P - D_j(RU_i u_j), + GRAV rho in z; the
+            // diagonal terms difference P + RU_i u_i in one go
+            double fu = -cx1 * (fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P)));
+            double fv = -cy1 * (fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P)));
+            double fw = fma(ro, c.GRAV, -cz1 * (fma(ZP(Q_RW), ZP(Q_W), ZP(Q_P)) - fma(ZM(Q_RW), ZM(Q_W), ZM(Q_P))));
             fu = fma(-cy1, fma(YP(Q_RU), YP(Q_V), -YM(Q_RU) * YM(Q_V)), fu);
             fu = fma(-cz1, fma(ZP(Q_RU), ZP(Q_W), -ZM(Q_RU) * ZM(Q_W)), fu);
             fv = fma(-cx1, fma(XP(Q_RV), XP(Q_U), -XM(Q_RV) * XM(Q_U)), fv);
-            fv = fma(-cy1, fma(YP(Q_RV), YP(Q_V), -YM(Q_RV) * YM(Q_V)), fv);
             fv = fma(-cz1, fma(ZP(Q_RV), ZP(Q_W), -ZM(Q_RV) * ZM(Q_W)), fv);
             fw = fma(-cx1, fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U)), fw);
             fw = fma(-cy1, fma(YP(Q_RW), YP(Q_V), -YM(Q_RW) * YM(Q_V)), fw);
-            fw = fma(-cz1, fma(ZP(Q_RW), ZP(Q_W), -ZM(Q_RW) * ZM(Q_W)), fw);
 
             // ---- temperature: advection (3dmhdsub.h:293-296), conduction (:315-319)
-            const double Tz = Dz(Q_TT);
+            const double dTz = ZP(Q_TT) - ZM(Q_TT);
+            const double Tz = dTz * cz1;  // without lShr only (advection)
             double ft;
             if constexpr (!SW::lShr) {
                 ft = -fma(u, Dx(Q_TT), fma(v, Dy(Q_TT), w * Tz));
@@ -255,7 +253,11 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     // as lap T + (HRAD - d2 TTM/dz2), the latter precomputed per z
                     ft = fma(ri * (c.OCV / c.REPR), lapT + c.lrem_g[z], ft);
                 } else {
-                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+                    if constexpr (SW::lShr) {
+                        ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
+                    } else {
+                        ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+                    }
                 }
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
