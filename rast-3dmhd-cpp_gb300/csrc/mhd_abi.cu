@@ -582,6 +582,17 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         const double kx13 = c13ore * h[base_off[0] + 1], ky13 = c13ore * h[base_off[1] + 1];
         for (int z = 0; z < nz; z++) h.push_back(kx13 * h[base_off[2] + z]);
         for (int z = 0; z < nz; z++) h.push_back(ky13 * h[base_off[2] + z]);
+        // OBETA cz1; the conduction coefficients with kapz folded in (uniform x / y)
+        for (int z = 0; z < nz; z++) h.push_back(ctx->k.OBETA * h[base_off[2] + z]);
+        const double cx2b = h[base_off[0] + 2 * (size_t)nx + 1], cy2b = h[base_off[1] + 2 * (size_t)ny + 1];
+        for (int t = 0; t < 5; t++)
+            for (int z = 0; z < nz; z++) {
+                const double kz = h[kap_off + z], dkz = h[kap_off + nz + z];
+                const double cz1 = h[base_off[2] + z], cz2a = h[base_off[2] + nz + z], cz2b = h[base_off[2] + 2 * (size_t)nz + z];
+                const double v[5] = {kz * cx2b, kz * cy2b, kz * cz2b, kz * cz2a + dkz * cz1,
+                                     kz * (2.0 * (cx2b + cy2b + cz2b))};
+                h.push_back(v[t]);
+            }
     }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -613,6 +624,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lap_off + (size_t)set * nz;
         ctx->coef.kxz = b0 + lap_off + 6 * (size_t)nz;
         ctx->coef.kyz = b0 + lap_off + 7 * (size_t)nz;
+        ctx->coef.ocz1 = b0 + lap_off + 8 * (size_t)nz;
+        for (int t = 0; t < 5; t++) ctx->coef.condT[t] = b0 + lap_off + (size_t)(9 + t) * nz;
     }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;

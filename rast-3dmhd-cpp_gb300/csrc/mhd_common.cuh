@@ -81,6 +81,9 @@ struct Coefs {
     const double* s2[3][6];
     const double *kapz, *dkapz;  // (OCV/REPR)*RKAPA[z], (OCV/REPR)*DKAPA[z]
     const double* dkz;           // dkapz[z] * cz1[z]
+    const double* ocz1;          // OBETA * cz1[z]
+    // with uniform_xy, per z: kapz*cx2b, kapz*cy2b, kapz*cz2b, kapz*cz2a + dkapz*cz1, kapz*S_T
+    const double* condT[5];
     // uniform x and y grids: d2xxdx2 and d2yydy2 vanish and the x / y
     // coefficients are the same in every interior column
     int uniform_xy;

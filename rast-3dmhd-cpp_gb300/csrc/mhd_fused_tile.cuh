@@ -167,6 +167,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
     const bool halted = a.dtp && a.dtp[3] != 0.0;
     const double ocvore = c.OCV * c.ORE;
     const double ohm = c.OBETA * c.ORM * c.OCV;
+    // with lShr the current density carries OBETA (j' = OBETA j): the Lorentz force
+    // is B x j' and the Ohmic heating (ORM OCV / OBETA) |j'|^2
+    const double ocx1 = c.OBETA * cx1, ocy1 = c.OBETA * cy1;
+    const double ohm2 = c.OBETA != 0.0 ? c.ORM * c.OCV / c.OBETA : 0.0;
 
     load_plane<SW, T>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
     load_plane<SW, T>(a, ring, zb % 3, zb, x0, y0);
@@ -240,9 +244,9 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 ft = a.FT[i];  // the reference never re-initialises FT with lShr
             }
             {
-                double lapT;
+                double lapT = 0.0;
                 if constexpr (UXY) {
-                    lapT = lap3(0.0, Q_TT, cx2b, cy2b, cz2a, cz2b, K.lapS[3][z]);
+                    if (EXTRA && c.lrem && !SW::lShr) lapT = lap3(0.0, Q_TT, cx2b, cy2b, cz2a, cz2b, K.lapS[3][z]);
                 } else {
                     lapT = acc_d2<true>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
                     lapT = acc_d2<true>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
@@ -252,12 +256,18 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     // lRem: conduction of T - TTM(z) plus HRAD (3dmhdsub.h:297-313),
                     // as lap T + (HRAD - d2 TTM/dz2), the latter precomputed per z
                     ft = fma(ri * (c.OCV / c.REPR), lapT + c.lrem_g[z], ft);
+                } else if constexpr (UXY) {
+                    // kapz lap T + dkapz dT/dz with kapz folded into per-z coefficients:
+                    // condT = kapz (cx2b, cy2b, cz2b), kapz cz2a + dkapz cz1, kapz S
+                    double q = dTz * K.condT[3][z];
+                    q = fma(XP(Q_TT) + XM(Q_TT), K.condT[0][z], q);
+                    q = fma(YP(Q_TT) + YM(Q_TT), K.condT[1][z], q);
+                    q = fma(ZP(Q_TT) + ZM(Q_TT), K.condT[2][z], q);
+                    ft = fma(ri, fma(-C0(Q_TT), K.condT[4][z], q), ft);
+                } else if constexpr (SW::lShr) {
+                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
                 } else {
-                    if constexpr (SW::lShr) {
-                        ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
-                    } else {
-                        ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
-                    }
+                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
                 }
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
@@ -360,9 +370,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                              fma(-cyv, dBYy, cz1 * fma(bz, dVz, fma(-w, dBYz, -by * dWz))));
                     w3 = fma(cx1, fma(bx, dWx, fma(-u, dBZx, -bz * dUx)),
                              fma(cy1, fma(by, dWy, fma(-v, dBZy, -bz * dVy)), -czw * dBZz));
-                    jz = fma(cx1, dBYx, -cy1 * dBXy);
-                    jy = fma(cz1, dBXz, -cx1 * dBZx);
-                    jx = fma(cy1, dBZy, -cz1 * dBYz);
+                    const double ocz1 = K.ocz1[z];  // OBETA cz1
+                    jz = fma(ocx1, dBYx, -ocy1 * dBXy);
+                    jy = fma(ocz1, dBXz, -ocx1 * dBZx);
+                    jx = fma(ocy1, dBZy, -ocz1 * dBYz);
                 } else {
                     // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
                     double wzm = wz;
@@ -418,10 +429,17 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     w1 += sg * (-3.0 * bx + 4.0 * X1 - X2) * d2 + (2.0 * bx - 5.0 * X1 + 4.0 * X2 - X3) * d1;
                     w2 += sg * (-3.0 * by + 4.0 * Y1 - Y2) * d2 + (2.0 * by - 5.0 * Y1 + 4.0 * Y2 - Y3) * d1;
                 }
-                fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
-                fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
-                fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
-                ft = fma(ohm * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+                if constexpr (SW::lShr) {
+                    fu = fma(bz, jy, fma(-by, jz, fu));
+                    fv = fma(bx, jz, fma(-bz, jx, fv));
+                    fw = fma(by, jx, fma(-bx, jy, fw));
+                    ft = fma(ohm2 * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+                } else {
+                    fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
+                    fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
+                    fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
+                    ft = fma(ohm * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+                }
             }
 
             // ---- RK3 substage update and the next register (3dmhdsub.h:168-192)
