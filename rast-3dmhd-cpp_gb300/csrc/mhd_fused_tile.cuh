@@ -238,6 +238,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             const double dTz = ZP(Q_TT) - ZM(Q_TT);
             const double Tz = dTz * cz1;  // without lShr only (advection)
             double ft;
+            double qr = 0.0;  // the temperature terms proportional to 1/rho, applied once at the end
             if constexpr (!SW::lShr) {
                 ft = -fma(u, Dx(Q_TT), fma(v, Dy(Q_TT), w * Tz));
             } else {
@@ -263,7 +264,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     q = fma(XP(Q_TT) + XM(Q_TT), K.condT[0][z], q);
                     q = fma(YP(Q_TT) + YM(Q_TT), K.condT[1][z], q);
                     q = fma(ZP(Q_TT) + ZM(Q_TT), K.condT[2][z], q);
-                    ft = fma(ri, fma(-C0(Q_TT), K.condT[4][z], q), ft);
+                    qr = fma(-C0(Q_TT), K.condT[4][z], q);
                 } else if constexpr (SW::lShr) {
                     ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
                 } else {
@@ -272,7 +273,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
             if constexpr (EXTRA) {
-                if (c.pl_mode == 3) ft = fma(-c.pl_s * ri, c.plx[x] * c.ply[y] * c.plz[z], ft);
+                if (c.pl_mode == 3) qr = fma(-c.pl_s, c.plx[x] * c.ply[y] * c.plz[z], qr);
             }
 
             // ---- viscous Laplacians (3dmhdsub.h:462-472); scale pairs sx[2k], sx[2k+1]
@@ -326,7 +327,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 const double s1 = uy + vx, s2 = uz + wx, s3 = vz + wy;
                 const double sh = fma(s1, s1, fma(s2, s2, s3 * s3));
                 const double phi = fma(c.C43, dg, sh);
-                ft = fma(ocvore * ri, phi, ft);
+                qr = fma(ocvore, phi, qr);
                 ft = fma(-c.OCV * tt, ux + vy + wz, ft);
             }
 
@@ -433,14 +434,16 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     fu = fma(bz, jy, fma(-by, jz, fu));
                     fv = fma(bx, jz, fma(-bz, jx, fv));
                     fw = fma(by, jx, fma(-bx, jy, fw));
-                    ft = fma(ohm2 * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+                    qr = fma(ohm2, fma(jx, jx, fma(jy, jy, jz * jz)), qr);
                 } else {
                     fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
                     fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
                     fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
-                    ft = fma(ohm * ri, fma(jx, jx, fma(jy, jy, jz * jz)), ft);
+                    qr = fma(ohm, fma(jx, jx, fma(jy, jy, jz * jz)), qr);
                 }
             }
+
+            ft = fma(ri, qr, ft);
 
             // ---- RK3 substage update and the next register (3dmhdsub.h:168-192)
             const double fl[8] = {fu, fv, fw, ft, fr, w1, w2, w3};
