@@ -589,10 +589,19 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
             for (int z = 0; z < nz; z++) {
                 const double kz = h[kap_off + z], dkz = h[kap_off + nz + z];
                 const double cz1 = h[base_off[2] + z], cz2a = h[base_off[2] + nz + z], cz2b = h[base_off[2] + 2 * (size_t)nz + z];
-                const double v[5] = {kz * cx2b, kz * cy2b, kz * cz2b, kz * cz2a + dkz * cz1,
-                                     kz * (2.0 * (cx2b + cy2b + cz2b))};
+                const double v[5] = {kz * cx2b, kz * cy2b, kz * (cz2b + cz2a) + dkz * cz1,
+                                     kz * (cz2b - cz2a) - dkz * cz1, kz * (2.0 * (cx2b + cy2b + cz2b))};
                 h.push_back(v[t]);
             }
+        // z second-derivative factors of the points above and below, per scale pair
+        for (int k = 0; k < 4; k++)
+            for (int pm = 0; pm < 2; pm++)
+                for (int z = 0; z < nz; z++) {
+                    const double za = k < 3 ? h[scaled_off[2] + (size_t)(2 * k) * nz + z] : h[base_off[2] + nz + z];
+                    const double zb = k < 3 ? h[scaled_off[2] + (size_t)(2 * k + 1) * nz + z]
+                                            : h[base_off[2] + 2 * (size_t)nz + z];
+                    h.push_back(pm == 0 ? zb + za : zb - za);
+                }
     }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -626,6 +635,7 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         ctx->coef.kyz = b0 + lap_off + 7 * (size_t)nz;
         ctx->coef.ocz1 = b0 + lap_off + 8 * (size_t)nz;
         for (int t = 0; t < 5; t++) ctx->coef.condT[t] = b0 + lap_off + (size_t)(9 + t) * nz;
+        for (int t = 0; t < 8; t++) ctx->coef.lapZ[t] = b0 + lap_off + (size_t)(14 + t) * nz;
     }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;

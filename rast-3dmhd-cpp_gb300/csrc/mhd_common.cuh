@@ -82,8 +82,12 @@ struct Coefs {
     const double *kapz, *dkapz;  // (OCV/REPR)*RKAPA[z], (OCV/REPR)*DKAPA[z]
     const double* dkz;           // dkapz[z] * cz1[z]
     const double* ocz1;          // OBETA * cz1[z]
-    // with uniform_xy, per z: kapz*cx2b, kapz*cy2b, kapz*cz2b, kapz*cz2a + dkapz*cz1, kapz*S_T
+    // with uniform_xy, per z: kapz*cx2b, kapz*cy2b, then the factors of T(z+1) and T(z-1)
+    // kapz*(cz2b + cz2a) + dkapz*cz1 and kapz*(cz2b - cz2a) - dkapz*cz1, and kapz*S_T
     const double* condT[5];
+    // per z, for the scale pairs k = 0, 1, 2 (ORE, ORE*C43, ORM) and unscaled (k = 3):
+    // lapZ[2k] = b + a, lapZ[2k+1] = b - a of the z second-derivative coefficients
+    const double* lapZ[8];
     // uniform x and y grids: d2xxdx2 and d2yydy2 vanish and the x / y
     // coefficients are the same in every interior column
     int uniform_xy;

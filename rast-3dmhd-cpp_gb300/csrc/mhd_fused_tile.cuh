@@ -203,11 +203,13 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             auto lapz = [&](double acc, int q, int k) { return acc_d2<true>(acc, ZP(q), ZM(q), C0(q), sz[2 * k], sz[2 * k + 1]); };
             // uniform x / y: acc + sxb (px + mx) + syb (py + my) + (sza (pz - mz) + szb (pz + mz)) - c S,
             // S = 2 (sxb + syb + szb) from the per-z table: one -2c product for the three axes
-            auto lap3 = [&](double acc, int q, double sxb, double syb, double sza, double szb, double S) {
-                acc = fma(ZP(q) - ZM(q), sza, acc);
+            // the z part sza (pz - mz) + szb (pz + mz) as pz (szb + sza) + mz (szb - sza): szpm
+            // points at the per-z pair of tables
+            auto lap3 = [&](double acc, int q, double sxb, double syb, const double* const* szpm, double S) {
+                acc = fma(ZP(q), szpm[0][z], acc);
+                acc = fma(ZM(q), szpm[1][z], acc);
                 acc = fma(XP(q) + XM(q), sxb, acc);
                 acc = fma(YP(q) + YM(q), syb, acc);
-                acc = fma(ZP(q) + ZM(q), szb, acc);
                 return fma(-C0(q), S, acc);
             };
 
@@ -247,7 +249,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             {
                 double lapT = 0.0;
                 if constexpr (UXY) {
-                    if (EXTRA && c.lrem && !SW::lShr) lapT = lap3(0.0, Q_TT, cx2b, cy2b, cz2a, cz2b, K.lapS[3][z]);
+                    if (EXTRA && c.lrem && !SW::lShr) lapT = lap3(0.0, Q_TT, cx2b, cy2b, K.lapZ + 6, K.lapS[3][z]);
                 } else {
                     lapT = acc_d2<true>(0.0, XP(Q_TT), XM(Q_TT), C0(Q_TT), cx2a, cx2b);
                     lapT = acc_d2<true>(lapT, YP(Q_TT), YM(Q_TT), C0(Q_TT), cy2a, cy2b);
@@ -259,11 +261,12 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     ft = fma(ri * (c.OCV / c.REPR), lapT + c.lrem_g[z], ft);
                 } else if constexpr (UXY) {
                     // kapz lap T + dkapz dT/dz with kapz folded into per-z coefficients:
-                    // condT = kapz (cx2b, cy2b, cz2b), kapz cz2a + dkapz cz1, kapz S
-                    double q = dTz * K.condT[3][z];
+                    // condT = kapz (cx2b, cy2b), the pz and mz factors kapz (cz2b + cz2a) + dkapz cz1
+                    // and kapz (cz2b - cz2a) - dkapz cz1, and kapz S
+                    double q = ZP(Q_TT) * K.condT[2][z];
+                    q = fma(ZM(Q_TT), K.condT[3][z], q);
                     q = fma(XP(Q_TT) + XM(Q_TT), K.condT[0][z], q);
                     q = fma(YP(Q_TT) + YM(Q_TT), K.condT[1][z], q);
-                    q = fma(ZP(Q_TT) + ZM(Q_TT), K.condT[2][z], q);
                     qr = fma(-C0(Q_TT), K.condT[4][z], q);
                 } else if constexpr (SW::lShr) {
                     ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
@@ -278,9 +281,9 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
 
             // ---- viscous Laplacians (3dmhdsub.h:462-472); scale pairs sx[2k], sx[2k+1]
             if constexpr (UXY) {
-                fu = lap3(fu, Q_U, sx[3], sy[1], sz[0], sz[1], K.lapS[0][z]);
-                fv = lap3(fv, Q_V, sx[1], sy[3], sz[0], sz[1], K.lapS[1][z]);
-                fw = lap3(fw, Q_W, sx[1], sy[1], sz[2], sz[3], K.lapS[2][z]);
+                fu = lap3(fu, Q_U, sx[3], sy[1], K.lapZ + 0, K.lapS[0][z]);
+                fv = lap3(fv, Q_V, sx[1], sy[3], K.lapZ + 0, K.lapS[1][z]);
+                fw = lap3(fw, Q_W, sx[1], sy[1], K.lapZ + 2, K.lapS[2][z]);
             } else {
                 fu = lapz(lapy(lapx(fu, Q_U, 1), Q_U, 0), Q_U, 0);
                 fv = lapz(lapy(lapx(fv, Q_V, 0), Q_V, 1), Q_V, 0);
@@ -401,14 +404,14 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 }
                 const bool wall = (z == zl || z == zr - 1);
                 if constexpr (UXY) {
-                    w3 = lap3(w3, Q_BZ, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
+                    w3 = lap3(w3, Q_BZ, sx[5], sy[5], K.lapZ + 4, K.lapS[4][z]);
                     if (wall) {
                         // x and y parts only: acc + sxb (px + mx) + syb (py + my) - c 2 (sxb + syb)
                         w1 = fma(-bx, K.lapS[5][z], fma(YP(Q_BX) + YM(Q_BX), sy[5], fma(XP(Q_BX) + XM(Q_BX), sx[5], w1)));
                         w2 = fma(-by, K.lapS[5][z], fma(YP(Q_BY) + YM(Q_BY), sy[5], fma(XP(Q_BY) + XM(Q_BY), sx[5], w2)));
                     } else {
-                        w1 = lap3(w1, Q_BX, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
-                        w2 = lap3(w2, Q_BY, sx[5], sy[5], sz[4], sz[5], K.lapS[4][z]);
+                        w1 = lap3(w1, Q_BX, sx[5], sy[5], K.lapZ + 4, K.lapS[4][z]);
+                        w2 = lap3(w2, Q_BY, sx[5], sy[5], K.lapZ + 4, K.lapS[4][z]);
                     }
                 } else {
                     w1 = lapy(lapx(w1, Q_BX, 2), Q_BX, 2);
