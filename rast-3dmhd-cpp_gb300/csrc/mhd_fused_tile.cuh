@@ -60,9 +60,14 @@ constexpr int nq() {
     return SW::lMag ? Q_N : Q_BX;
 }
 
+// per-point differences of the plane being computed, after the ring: the z
+// differences of u, v, w and the x differences of u, v (the viscous cross
+// terms difference them once more between neighbours)
+enum D { D_UZ = 0, D_VZ, D_WZ, D_UX, D_VX, D_N };
+
 template <class SW, class T>
 constexpr size_t ring_bytes() {
-    return (size_t)3 * nq<SW>() * T::kPlane * sizeof(double);
+    return ((size_t)3 * nq<SW>() + D_N) * T::kPlane * sizeof(double);
 }
 
 // 1/x by Newton's iteration for the reciprocal, r <- r + r(1 - x r), applied
@@ -76,8 +81,14 @@ __device__ __forceinline__ double recip(double x) {
     return fma(r, e, r);
 }
 
+// Load plane z into ring slot `slot` with its derived quantities.  With
+// `diffs`, also the differences of plane z-1 into the difference arrays: the
+// z differences at each point from this plane and plane z-2, which the same
+// thread loaded at the same point, and the x differences from plane z-1,
+// which a barrier has made visible since its load.
 template <class SW, class T>
-__device__ __forceinline__ void load_plane(const FusedArgs& a, double* ring, int slot, int z, int x0, int y0) {
+__device__ __forceinline__ void load_plane(const FusedArgs& a, double* ring, int slot, int z, int x0, int y0,
+                                           bool diffs) {
     constexpr int NQ = nq<SW>();
     constexpr int kPlane = T::kPlane, kPX = T::kPX, kThreads = T::kThreads;
     double* base = ring + (size_t)slot * NQ * kPlane;
@@ -96,10 +107,24 @@ __device__ __forceinline__ void load_plane(const FusedArgs& a, double* ring, int
         base[Q_TT * kPlane + k] = tt;
         base[Q_RO * kPlane + k] = ro;
         base[Q_RI * kPlane + k] = ri;
-        base[Q_U * kPlane + k] = ru * ri;
-        base[Q_V * kPlane + k] = rv * ri;
-        base[Q_W * kPlane + k] = rw * ri;
+        // the stored, rounded products (not contracted into the differences below)
+        const double uu = __dmul_rn(ru, ri), vv = __dmul_rn(rv, ri), ww = __dmul_rn(rw, ri);
+        base[Q_U * kPlane + k] = uu;
+        base[Q_V * kPlane + k] = vv;
+        base[Q_W * kPlane + k] = ww;
         base[Q_P * kPlane + k] = ro * tt;
+        if (diffs) {
+            const double* Pm2 = ring + (size_t)((slot + 1) % 3) * NQ * kPlane;  // plane z-2
+            const double* Pm1 = ring + (size_t)((slot + 2) % 3) * NQ * kPlane;  // plane z-1
+            double* Dp = ring + (size_t)3 * NQ * kPlane;
+            Dp[D_UZ * kPlane + k] = uu - Pm2[Q_U * kPlane + k];
+            Dp[D_VZ * kPlane + k] = vv - Pm2[Q_V * kPlane + k];
+            Dp[D_WZ * kPlane + k] = ww - Pm2[Q_W * kPlane + k];
+            if (hx >= 1 && hx <= kPX - 2) {
+                Dp[D_UX * kPlane + k] = Pm1[Q_U * kPlane + k + 1] - Pm1[Q_U * kPlane + k - 1];
+                Dp[D_VX * kPlane + k] = Pm1[Q_V * kPlane + k + 1] - Pm1[Q_V * kPlane + k - 1];
+            }
+        }
         if constexpr (SW::lMag) {
             base[Q_BX * kPlane + k] = a.U.p[S_BX][i];
             base[Q_BY * kPlane + k] = a.U.p[S_BY][i];
@@ -172,9 +197,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
     const double ocx1 = c.OBETA * cx1, ocy1 = c.OBETA * cy1;
     const double ohm2 = c.OBETA != 0.0 ? c.ORM * c.OCV / c.OBETA : 0.0;
 
-    load_plane<SW, T>(a, ring, (zb - 1) % 3, zb - 1, x0, y0);
-    load_plane<SW, T>(a, ring, zb % 3, zb, x0, y0);
-    load_plane<SW, T>(a, ring, (zb + 1) % 3, zb + 1, x0, y0);
+    load_plane<SW, T>(a, ring, (zb - 1) % 3, zb - 1, x0, y0, false);
+    load_plane<SW, T>(a, ring, zb % 3, zb, x0, y0, false);
+    __syncthreads();  // plane zb complete: its x differences come with the next load
+    load_plane<SW, T>(a, ring, (zb + 1) % 3, zb + 1, x0, y0, true);
 
     const int pc = (ty + 1) * kPX + (tx + 1);  // centre offset inside a plane
     for (int z = zb; z < ze; z++) {
@@ -190,6 +216,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             auto YM = [&](int q) { return P0[q * kPlane + pc - kPX]; };
             auto ZP = [&](int q) { return Pp[q * kPlane + pc]; };
             auto ZM = [&](int q) { return Pm[q * kPlane + pc]; };
+            const double* Dp = ring + (size_t)3 * NQ * kPlane;  // differences of plane z
+            auto DD = [&](int d, int off) { return Dp[d * kPlane + pc + off]; };
             const double cz1 = K.cz1[z], cz2a = K.cz2a[z], cz2b = K.cz2b[z];
             double sz[6];
 #pragma unroll
@@ -300,13 +328,13 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     kxz = kx13 * cz1;
                     kyz = ky13 * cz1;
                 }
-                auto E = [&](const double* Pl, int q, int off) { return Pl[q * kPlane + pc + off]; };
-                const double dyxv = (E(P0, Q_V, kPX + 1) - E(P0, Q_V, kPX - 1)) - (E(P0, Q_V, -kPX + 1) - E(P0, Q_V, -kPX - 1));
-                const double dyxu = (E(P0, Q_U, kPX + 1) - E(P0, Q_U, kPX - 1)) - (E(P0, Q_U, -kPX + 1) - E(P0, Q_U, -kPX - 1));
-                const double dxzw = (E(Pp, Q_W, 1) - E(Pm, Q_W, 1)) - (E(Pp, Q_W, -1) - E(Pm, Q_W, -1));
-                const double dyzw = (E(Pp, Q_W, kPX) - E(Pm, Q_W, kPX)) - (E(Pp, Q_W, -kPX) - E(Pm, Q_W, -kPX));
-                const double dxzu = (E(Pp, Q_U, 1) - E(Pm, Q_U, 1)) - (E(Pp, Q_U, -1) - E(Pm, Q_U, -1));
-                const double dyzv = (E(Pp, Q_V, kPX) - E(Pm, Q_V, kPX)) - (E(Pp, Q_V, -kPX) - E(Pm, Q_V, -kPX));
+                // mixed differences as differences of the neighbours' 1-D differences
+                const double dyxv = DD(D_VX, kPX) - DD(D_VX, -kPX);
+                const double dyxu = DD(D_UX, kPX) - DD(D_UX, -kPX);
+                const double dxzw = DD(D_WZ, 1) - DD(D_WZ, -1);
+                const double dyzw = DD(D_WZ, kPX) - DD(D_WZ, -kPX);
+                const double dxzu = DD(D_UZ, 1) - DD(D_UZ, -1);
+                const double dyzv = DD(D_VZ, kPX) - DD(D_VZ, -kPX);
                 fu = fma(kxy, dyxv, fma(kxz, dxzw, fu));
                 fv = fma(kxy, dyxu, fma(kyz, dyzw, fv));
                 fw = fma(kxz, dxzu, fma(kyz, dyzv, fw));
@@ -315,9 +343,9 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             // velocity gradients (heating and, without lShr, induction)
             double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
             if constexpr (!SW::lShr) {
-                ux = Dx(Q_U); uy = Dy(Q_U); uz = Dz(Q_U);
-                vx = Dx(Q_V); vy = Dy(Q_V); vz = Dz(Q_V);
-                wx = Dx(Q_W); wy = Dy(Q_W); wz = Dz(Q_W);
+                ux = DD(D_UX, 0) * cx1; uy = Dy(Q_U); uz = DD(D_UZ, 0) * cz1;
+                vx = DD(D_VX, 0) * cx1; vy = Dy(Q_V); vz = DD(D_VZ, 0) * cz1;
+                wx = Dx(Q_W); wy = Dy(Q_W); wz = DD(D_WZ, 0) * cz1;
             }
             // ---- viscous heating and pdV work (3dmhdsub.h:477-538, not with lShr)
             if constexpr (!SW::lShr) {
@@ -351,10 +379,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     // the velocity gradients feed the induction terms only: group each
                     // component's terms by axis over raw differences and apply the axis'
                     // metric factor once per group
-                    const double dUx = XP(Q_U) - XM(Q_U), dUy = YP(Q_U) - YM(Q_U), dUz = ZP(Q_U) - ZM(Q_U);
-                    const double dVx = XP(Q_V) - XM(Q_V), dVy = YP(Q_V) - YM(Q_V), dVz = ZP(Q_V) - ZM(Q_V);
+                    const double dUx = DD(D_UX, 0), dUy = YP(Q_U) - YM(Q_U), dUz = DD(D_UZ, 0);
+                    const double dVx = DD(D_VX, 0), dVy = YP(Q_V) - YM(Q_V), dVz = DD(D_VZ, 0);
                     const double dWx = XP(Q_W) - XM(Q_W), dWy = YP(Q_W) - YM(Q_W);
-                    double dWz = ZP(Q_W) - ZM(Q_W);
+                    double dWz = DD(D_WZ, 0);
                     // one-sided dw/dz on the walls for the induction terms (3dmhdsub.h:572-584)
                     if (z == zl) {
                         const long long j = i + 2 * g.sz;
@@ -464,7 +492,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             }
         }
         __syncthreads();
-        if (z + 2 <= ze) load_plane<SW, T>(a, ring, (z + 2) % 3, z + 2, x0, y0);
+        if (z + 2 <= ze) load_plane<SW, T>(a, ring, (z + 2) % 3, z + 2, x0, y0, true);
     }
 }
 
