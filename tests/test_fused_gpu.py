@@ -162,3 +162,32 @@ def test_config1_full_size_one_step(capsys):
         print("\n512x512x256 one fused step vs oracle, worst 64x64x32 block:", {k: f"{v:.1e}" for k, v in worst.items()})
     for k in STATE_FIELDS:
         assert errs[k] <= TOL_ONE_STEP and worst[k] <= TOL_ONE_STEP, k
+
+
+@pytest.mark.parametrize("mag,shr", [(True, True), (True, False), (False, True), (False, False)])
+def test_stretched_xy_grid_general_path(mag, shr):
+    """Caller-supplied non-uniform x/y metrics (tanh-stretched, d2xxdx2 and
+    d2yydy2 nonzero) run the general instantiation of the fused substage (the
+    uniform one relies on per-z tables); one step against the oracle fed the
+    same metric arrays."""
+    import oracle
+    from gpu_util import METRIC_NAMES
+    from mhd_gb300.case import tanh_metric
+    case = small_cases()["mhd_rot_flux"].replace(lMag=mag, lShr=shr, nPx=24, nPy=16, nPz=12)
+    dxm, dym = tanh_metric(case.nPx, case.xMax, 0.8), tanh_metric(case.nPy, case.yMax, 0.6)
+    mo = {"dxxdx": dxm[0], "d2xxdx2": dxm[1], "DDX": dxm[2], "dyydy": dym[0], "d2yydy2": dym[1], "DDY": dym[2]}
+    st = initial_state(case)
+    sim = Simulation(case, path="fused", metric_override=mo)
+    sim.upload_state(st)
+    sim.communicate()
+    sim.step(case.dt)
+    got = sim.download_state()
+    sim.close()
+    o = oracle.OracleSim(case, st)
+    for n, a in mo.items():
+        o._metric_arrays[METRIC_NAMES.index(n)][:] = a  # the oracle reads these arrays in place
+    o.communicate()
+    o.steps(1)
+    for k in STATE_FIELDS[:case.nfields]:
+        e = rel_err(got[k], o.arr[k])
+        assert e <= TOL_ONE_STEP, (k, e)
