@@ -23,8 +23,22 @@
 //   * UXY (uniform x and y grids: d2uudu2 = 0, the same coefficients in
 //     every column) drops the first-derivative part of the x/y second
 //     derivatives at compile time and sums each Laplacian as
-//     sx (px + mx) + sy (py + my) + sz (pz + mz) - c S with S = 2 (sx + sy + sz)
-//     from a per-z table: one -2c product instead of one per axis;
+//     sx (px + mx) + sy (py + my) + pz (szb + sza) + mz (szb - sza) - c S with
+//     S = 2 (sx + sy + szb) and the z factors from per-z tables: one -2c
+//     product instead of one per axis, no (pz - mz) / (pz + mz); the
+//     conduction coefficient kappa(z) and the DKAPA dT/dz term are folded
+//     into the temperature's tables, and the cross-term factors are per-z
+//     tables too;
+//   * with lShr (no temperature advection or heating) the velocity gradients
+//     feed only the induction terms, which are grouped per axis over raw
+//     differences with the metric factor applied once per group, and OBETA
+//     rides in the current density;
+//   * the pressure is differenced together with the diagonal momentum flux
+//     (P + RU_i u_i), and the temperature terms proportional to 1/rho are
+//     summed before one multiply;
+//   * load_plane forms per point the z differences of u, v, w and the x
+//     differences of u, v (difference arrays after the ring), from which the
+//     viscous mixed derivatives are one subtraction of two neighbours' values;
 //   * repeated gradients are computed once; 1/rho is Newton's iteration
 //     r <- r + r(1 - rho r), twice, from the hardware reciprocal estimate.
 // Results agree with the reference to rounding (1e-12 of each field's
