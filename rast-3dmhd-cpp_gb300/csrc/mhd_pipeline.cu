@@ -5,12 +5,15 @@
 // an upload and a download of the whole state around every step.  Here the
 // interior z planes are cut into slabs and the step runs as a dataflow over
 // five streams, one per kind of work:
-//   copy-in          slab j (all fields) -> U[cur], then event up[j]
-//   substage s=1..3  S_s(j) after the event of slab j+1 one stage before
-//                    (up[j+1] for S1, S1 done[j+1] for S2, S2 done[j+1] for S3)
+//   copy-in          slab j (all fields) and the first plane of slab j+1 -> U[cur],
+//                    then event up[j]
+//   substage s=1..3  S_s(j) after up[j] (S1), or after stage s-1 of slab j+1
+//                    (S1 done[j+1] for S2, S2 done[j+1] for S3)
 //   copy-out         slab j of the new state after S3 done[j]
 // Substage s of slab j reads its neighbours one plane beyond the slab, which
-// stage s-1 of slab j+1 has produced by then; the same event orders the
+// came with the slab's upload (S1) or which stage s-1 of slab j+1 has
+// produced by then (S2, S3: waiting for the whole slab j+1 of S1 would hold
+// S1 a slab behind the uploads for no reason); the same events order the
 // in-place ping-pong writes (S2(j) overwrites U[cur] planes that S1 of slabs
 // j-1..j+1 read, S3(j) overwrites U[1-cur] planes that S2 of slabs j-1..j+1
 // read), and the substages of one slab follow one another through it.  The
@@ -124,9 +127,11 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
     PCK(cudaStreamWaitEvent(ctx->s_up, start, 0));
     PCK(cudaStreamWaitEvent(ctx->s_down, start, 0));
     for (int s = 0; s < 3; s++) PCK(cudaStreamWaitEvent(ctx->s_sub[s], start, 0));
+    // up[j]: slab j and the first plane of slab j+1, all that S1 of slab j reads
+    auto up_hi = [&](int j) { return j == ns - 1 ? nz : hi_of(j) + 1; };
     for (int j = 0; j < ns; j++) {
         if (in) {
-            PCK(copy_planes(ctx, Uin, const_cast<double*>(in), lo_of(j), hi_of(j), true, ctx->s_up));
+            PCK(copy_planes(ctx, Uin, const_cast<double*>(in), j == 0 ? 0 : up_hi(j - 1), up_hi(j), true, ctx->s_up));
             // the z ghost planes are never written by a substage: both buffers hold them
             if (j == 0) PCK(copy_planes(ctx, Uout, const_cast<double*>(in), 0, 1, true, ctx->s_up));
             if (j == ns - 1) PCK(copy_planes(ctx, Uout, const_cast<double*>(in), nz - 1, nz, true, ctx->s_up));
@@ -152,7 +157,7 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
         for (int s = 0; s < 3; s++) {
             const int j = t - s;
             if (j < 0 || j >= ns) continue;
-            PCK(cudaStreamWaitEvent(ctx->s_sub[s], ev[s][std::min(j + 1, ns - 1)], 0));
+            PCK(cudaStreamWaitEvent(ctx->s_sub[s], ev[s][s == 0 ? j : std::min(j + 1, ns - 1)], 0));
             if ((rc = substage(s, j))) return rc;
             PCK(cudaEventRecord(ev[s + 1][j], ctx->s_sub[s]));
             if (s == 2 && out) {
