@@ -64,19 +64,22 @@ extern "C" int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double
         return ctxops::fail(ctx, MHD_ERR_UNSUPPORTED, "host-to-host steps run on the fused FP64 path");
     const int nPz = ctx->g.nz - 2, nz = ctx->g.nz;
     // Interior slab heights grow geometrically from the bottom wall, 4, 4, 8,
-    // 16, then about 32 planes, and shrink again, 16, 8, 4, at the top: the
-    // compute waits for the first two slabs' upload, each later upload must
-    // fit under the compute of the slabs before it (a plane uploads in about
-    // 0.7x the time its three substages take at 512 x 512), and the last
-    // download follows the last kernel.  Every slab has at least 4 planes (the
-    // wall stencils reach 3 planes in).
+    // 16, then about 32 planes, and shrink again, 24, 16, 12, 8, 4 (16, 8, 4
+    // below 128 planes), at the top: the compute waits for the first slab's
+    // upload, each later upload must fit under the compute of the slabs
+    // before it, and the downloads of the last slabs, which queue behind one
+    // another after the last kernels, are short.  Every slab has at least 4
+    // planes (the wall stencils reach 3 planes in).
     std::vector<int> b{1};
-    const int head[4] = {4, 4, 8, 16}, tail[3] = {16, 8, 4};
+    const int head[4] = {4, 4, 8, 16}, tail_long[5] = {24, 16, 12, 8, 4}, tail_short[3] = {16, 8, 4};
     if (nPz >= 92) {
+        const bool lt = nPz >= 32 + 64 + 32;
+        const int* tail = lt ? tail_long : tail_short;
+        const int nt = lt ? 5 : 3, st = lt ? 64 : 28;
         for (int h : head) b.push_back(b.back() + h);
-        const int mid = nPz - 32 - 28, nm = std::max(1, (mid + 16) / 32), m0 = b.back();
+        const int mid = nPz - 32 - st, nm = std::max(1, (mid + 16) / 32), m0 = b.back();
         for (int j = 1; j <= nm; j++) b.push_back(m0 + (int)((long long)mid * j / nm));
-        for (int h : tail) b.push_back(b.back() + h);
+        for (int t = 0; t < nt; t++) b.push_back(b.back() + tail[t]);
     }
     const int ns = (int)b.size() - 1;
     if (ns < 3 || ctx->c.lrem) {
