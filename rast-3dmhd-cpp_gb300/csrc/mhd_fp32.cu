@@ -138,6 +138,16 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
     const int pc = (ty + 1) * kPX + (tx + 1);
     for (int z = zb; z < ze; z++) {
         __syncthreads();
+        if (z + 2 <= ze) {  // the points of plane z+2 this thread loads after the compute below
+            for (int k = threadIdx.x; k < kPlane; k += kThreads) {
+                const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
+                if (gx >= g.nx || gy >= g.ny) continue;
+                const long long ip = (long long)(z + 2) * g.sz + (long long)gy * g.sy + gx;
+                constexpr int nfp = SW::lMag ? 8 : 5;
+#pragma unroll
+                for (int f = 0; f < nfp; f++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.U.p[f] + ip));
+            }
+        }
         if (active) {
             const RingPtrs Rm = ring_slot<SW>(ring, (z - 1) % 3);
             const RingPtrs R0 = ring_slot<SW>(ring, z % 3);
@@ -172,6 +182,14 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             };
 
             const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
+            // bring the next plane's FP64 register (and FT) into L2 while this cell computes
+            if (z + 1 < ze) {
+                const long long inx = i + g.sz;
+                constexpr int nfp = SW::lMag ? 8 : 5;
+#pragma unroll
+                for (int f = 0; f < nfp; f++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Z.p[f] + inx));
+                if constexpr (SW::lShr) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.FT + inx));
+            }
             const double ro = a.bgR[z] + widen_f32(C0(F_DRO));
             const double tt = a.bgT[z] + widen_f32(C0(F_DT));
             const float ri = C0(F_RI), ttf = narrow_f64(tt);
