@@ -20,6 +20,8 @@
 #include "mhd_common.cuh"
 #include "mhd_convert.cuh"
 
+#include <type_traits>
+
 namespace mhd {
 namespace {
 
@@ -328,18 +330,24 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                                   widen_f32(fr), widen_f32(w1), widen_f32(w2), widen_f32(w3)};
             const int nf = SW::lMag ? 8 : 5;
             const double r0z = a.bgR[z], t0z = a.bgT[z];
+            // Z carries the full FP64 state across steps (written by substage 3
+            // and by BCON), so substage 1 starts from it instead of from the
+            // FP32 copy: step_block_ZETA0 without the FP32 rounding.  The last
+            // substage (and a halted record) stores U' itself into Z; the split
+            // keeps its unused register update off the FP64 pipe.
+            auto epilogue = [&](auto next_register) {
 #pragma unroll
-            for (int f = 0; f < 8; f++) {
-                if (f >= nf) break;
-                // Z carries the full FP64 state across steps (written by substage 3
-                // and by BCON), so substage 1 starts from it instead of from the
-                // FP32 copy: step_block_ZETA0 without the FP32 rounding.
-                const double zf = a.Z.p[f][i];
-                const double un = halted ? zf : fma(gdt, fl[f], zf);
-                const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
-                store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
-                a.Z.p[f][i] = (a.substage < 2 && !halted) ? fma(zdt, fl[f], un) : un;
-            }
+                for (int f = 0; f < 8; f++) {
+                    if (f >= nf) break;
+                    const double zf = a.Z.p[f][i];
+                    const double un = halted ? zf : fma(gdt, fl[f], zf);
+                    const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
+                    store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
+                    a.Z.p[f][i] = next_register ? fma(zdt, fl[f], un) : un;
+                }
+            };
+            if (a.substage < 2 && !halted) epilogue(std::true_type{});
+            else epilogue(std::false_type{});
             if constexpr (SW::lShr) {
                 if (!halted) a.FT[i] = ftd;
             }
