@@ -117,16 +117,22 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
 
     const int xc = active ? x : 1, yc = active ? y : 1;
     const double cx1d = a.k.cx1[xc], cy1d = a.k.cy1[yc];
-    const float cx1 = (float)cx1d, cx2a = (float)a.k.cx2a[xc], cx2b = (float)a.k.cx2b[xc];
-    const float cy1 = (float)cy1d, cy2a = (float)a.k.cy2a[yc], cy2b = (float)a.k.cy2b[yc];
-    const float c13ore = (float)(c.C13 * c.ORE);
-    const float kxy = (float)(c.C13 * c.ORE * cx1d * cy1d);
-    const float ore = (float)c.ORE, ore43 = (float)(c.ORE * c.C43);
-    const float ocvore = (float)(c.OCV * c.ORE), ocv = (float)c.OCV;
-    const float ohm = (float)(c.OBETA * c.ORM * c.OCV);
-    const float tmpc = (float)(c.OCV / c.REPR);
-    const float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
-    const float omz = (float)c.OMZ, omx = (float)c.OMX;
+    float cx1 = (float)cx1d, cx2a = (float)a.k.cx2a[xc], cx2b = (float)a.k.cx2b[xc];
+    float cy1 = (float)cy1d, cy2a = (float)a.k.cy2a[yc], cy2b = (float)a.k.cy2b[yc];
+    float c13ore = (float)(c.C13 * c.ORE);
+    float kxy = (float)(c.C13 * c.ORE * cx1d * cy1d);
+    float ore = (float)c.ORE, ore43 = (float)(c.ORE * c.C43);
+    float ocvore = (float)(c.OCV * c.ORE), ocv = (float)c.OCV;
+    float ohm = (float)(c.OBETA * c.ORM * c.OCV);
+    float tmpc = (float)(c.OCV / c.REPR);
+    float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
+    float omz = (float)c.OMZ, omx = (float)c.OMX;
+    // GB300 runs float<->double conversions on its FP64 pipe; under the 80-register
+    // cap the compiler would recompute these converted constants inside the z loop
+    // (12 conversions per cell, measured).  Opaque copies stay in registers instead.
+    asm volatile("" : "+f"(omz), "+f"(omx), "+f"(cx1), "+f"(cx2a), "+f"(cx2b), "+f"(cy1), "+f"(cy2a), "+f"(cy2b));
+    asm volatile("" : "+f"(c13ore), "+f"(kxy), "+f"(ore), "+f"(ore43), "+f"(ocvore), "+f"(ocv), "+f"(ohm), "+f"(tmpc));
+    asm volatile("" : "+f"(obeta), "+f"(orm), "+f"(c43));
     // RK coefficients: from the host, or from the device time-step record; a
     // halted record (dt below 1e-8) turns the substage into a copy of the state
     const double gdt = a.dtp ? a.gam * a.dtp[0] : a.gdt;
