@@ -13,9 +13,15 @@ namespace mhd {
 namespace {
 
 using namespace fused;
-// tile height of the single-instance kernel (32 x MHD_FUSED_TILE_Y threads)
+// tile of the single-instance kernel (MHD_FUSED_TILE_X x MHD_FUSED_TILE_Y threads):
+// 16 x 8 loads 18 x 10 ring points per 128 cells (32 x 4: 34 x 6), and each
+// warp still reads whole 128-byte rows (measured: 71.7 vs 72.9 ms per step at
+// 512 x 512 x 256; 32 x 6, 32 x 8 and 16 x 12 run fewer CTAs per SM and are slower)
+#ifndef MHD_FUSED_TILE_X
+#define MHD_FUSED_TILE_X 16
+#endif
 #ifndef MHD_FUSED_TILE_Y
-#define MHD_FUSED_TILE_Y 4
+#define MHD_FUSED_TILE_Y 8
 #endif
 // This file is compiled twice: MHD_FUSED_XP=0 gives the kernels without the
 // optional temperature terms (and the dispatcher and the wall kernels),
@@ -24,7 +30,7 @@ using namespace fused;
 #define MHD_FUSED_XP 0
 #endif
 constexpr bool kExtra = MHD_FUSED_XP != 0;
-using DefaultTile = Tile<32, MHD_FUSED_TILE_Y>;
+using DefaultTile = Tile<MHD_FUSED_TILE_X, MHD_FUSED_TILE_Y>;
 constexpr int kMinBlocks = DefaultTile::kThreads >= 256 ? 2 : 3;
 
 template <class SW, bool UXY>
