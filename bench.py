@@ -556,7 +556,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-step-scale", type=int, default=10)
     ap.add_argument("--precision-steps", type=int, default=1000)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     dist = Dist()
