@@ -564,44 +564,55 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         uxy = same(base_off[ax], ns[ax]) && same(base_off[ax] + 2 * (size_t)ns[ax], ns[ax]);
         for (int k = 1; k < 6 && uxy; k += 2) uxy = same(scaled_off[ax] + (size_t)k * ns[ax], ns[ax]);
     }
-    // per-z sums of the Laplacians' 'b' coefficients (used with uniform x / y grids)
-    const size_t lap_off = h.size();
+    // Per-z tables of the fused substage on uniform x / y grids (the x / y
+    // coefficients are then the interior column 1's); each records its offset.
+    auto push_z = [&](auto value_at) {
+        const size_t off = h.size();
+        for (int z = 0; z < nz; z++) h.push_back(value_at(z));
+        return off;
+    };
+    auto c1 = [&](int ax, int i) { return h[base_off[ax] + i]; };
+    auto c2a = [&](int ax, int i) { return h[base_off[ax] + (size_t)ns[ax] + i]; };
+    auto c2b = [&](int ax, int i) { return h[base_off[ax] + 2 * (size_t)ns[ax] + i]; };
+    auto s2a = [&](int ax, int k, int i) { return h[scaled_off[ax] + (size_t)(2 * k) * ns[ax] + i]; };
+    auto s2b = [&](int ax, int k, int i) { return h[scaled_off[ax] + (size_t)(2 * k + 1) * ns[ax] + i]; };
+    size_t lapS_off[6], condT_off[5], lapZ_off[8];
+    // S = 2 (sx + sy + sz) of the Laplacians of u, v, w (viscous scales, C43 on the x, y, z
+    // axis), T (unscaled), B (resistive), and 2 (sx + sy) of B on the wall planes
     {
-        auto sb = [&](int ax, int k, int i) { return h[scaled_off[ax] + (size_t)(2 * k + 1) * ns[ax] + i]; };
-        auto pb = [&](int ax, int i) { return h[base_off[ax] + 2 * (size_t)ns[ax] + i]; };
         const int kx[6] = {1, 0, 0, -1, 2, 2}, ky[6] = {0, 1, 0, -1, 2, 2}, kz[6] = {0, 0, 1, -1, 2, -2};
         for (int set = 0; set < 6; set++)
-            for (int z = 0; z < nz; z++) {
-                const double sx = kx[set] < 0 ? pb(0, 1) : sb(0, kx[set], 1);
-                const double sy = ky[set] < 0 ? pb(1, 1) : sb(1, ky[set], 1);
-                const double sz = kz[set] == -2 ? 0.0 : kz[set] < 0 ? pb(2, z) : sb(2, kz[set], z);
-                h.push_back(2.0 * (sx + sy + sz));
-            }
-        // the kernel's C13*ORE*cx1*cz1 and C13*ORE*cy1*cz1, same order of operations
-        const double c13ore = ctx->k.C13 * ctx->k.ORE;
-        const double kx13 = c13ore * h[base_off[0] + 1], ky13 = c13ore * h[base_off[1] + 1];
-        for (int z = 0; z < nz; z++) h.push_back(kx13 * h[base_off[2] + z]);
-        for (int z = 0; z < nz; z++) h.push_back(ky13 * h[base_off[2] + z]);
-        // OBETA cz1; the conduction coefficients with kapz folded in (uniform x / y)
-        for (int z = 0; z < nz; z++) h.push_back(ctx->k.OBETA * h[base_off[2] + z]);
-        const double cx2b = h[base_off[0] + 2 * (size_t)nx + 1], cy2b = h[base_off[1] + 2 * (size_t)ny + 1];
-        for (int t = 0; t < 5; t++)
-            for (int z = 0; z < nz; z++) {
-                const double kz = h[kap_off + z], dkz = h[kap_off + nz + z];
-                const double cz1 = h[base_off[2] + z], cz2a = h[base_off[2] + nz + z], cz2b = h[base_off[2] + 2 * (size_t)nz + z];
-                const double v[5] = {kz * cx2b, kz * cy2b, kz * (cz2b + cz2a) + dkz * cz1,
-                                     kz * (cz2b - cz2a) - dkz * cz1, kz * (2.0 * (cx2b + cy2b + cz2b))};
-                h.push_back(v[t]);
-            }
-        // z second-derivative factors of the points above and below, per scale pair
-        for (int k = 0; k < 4; k++)
-            for (int pm = 0; pm < 2; pm++)
-                for (int z = 0; z < nz; z++) {
-                    const double za = k < 3 ? h[scaled_off[2] + (size_t)(2 * k) * nz + z] : h[base_off[2] + nz + z];
-                    const double zb = k < 3 ? h[scaled_off[2] + (size_t)(2 * k + 1) * nz + z]
-                                            : h[base_off[2] + 2 * (size_t)nz + z];
-                    h.push_back(pm == 0 ? zb + za : zb - za);
-                }
+            lapS_off[set] = push_z([&](int z) {
+                const double sx = kx[set] < 0 ? c2b(0, 1) : s2b(0, kx[set], 1);
+                const double sy = ky[set] < 0 ? c2b(1, 1) : s2b(1, ky[set], 1);
+                const double sz = kz[set] == -2 ? 0.0 : kz[set] < 0 ? c2b(2, z) : s2b(2, kz[set], z);
+                return 2.0 * (sx + sy + sz);
+            });
+    }
+    // the viscous cross-term factors C13*ORE*cx1*cz1, C13*ORE*cy1*cz1 (the kernel's order)
+    const double c13ore = ctx->k.C13 * ctx->k.ORE;
+    const double kx13 = c13ore * c1(0, 1), ky13 = c13ore * c1(1, 1);
+    const size_t kxz_off = push_z([&](int z) { return kx13 * c1(2, z); });
+    const size_t kyz_off = push_z([&](int z) { return ky13 * c1(2, z); });
+    const size_t ocz1_off = push_z([&](int z) { return ctx->k.OBETA * c1(2, z); });
+    // conduction with kapz folded in: kapz cx2b, kapz cy2b, the factors of T(z+1) and
+    // T(z-1) kapz (cz2b +- cz2a) +- dkapz cz1, and kapz S_T
+    {
+        auto kz = [&](int z) { return h[kap_off + z]; };
+        auto dkz = [&](int z) { return h[kap_off + nz + z]; };
+        condT_off[0] = push_z([&](int z) { return kz(z) * c2b(0, 1); });
+        condT_off[1] = push_z([&](int z) { return kz(z) * c2b(1, 1); });
+        condT_off[2] = push_z([&](int z) { return kz(z) * (c2b(2, z) + c2a(2, z)) + dkz(z) * c1(2, z); });
+        condT_off[3] = push_z([&](int z) { return kz(z) * (c2b(2, z) - c2a(2, z)) - dkz(z) * c1(2, z); });
+        condT_off[4] = push_z([&](int z) { return kz(z) * (2.0 * (c2b(0, 1) + c2b(1, 1) + c2b(2, z))); });
+    }
+    // z second-derivative factors b + a and b - a of the planes above and below, for the
+    // scale pairs k = 0, 1, 2 (ORE, ORE*C43, ORM) and unscaled (k = 3)
+    for (int k = 0; k < 4; k++) {
+        auto za = [&](int z) { return k < 3 ? s2a(2, k, z) : c2a(2, z); };
+        auto zb = [&](int z) { return k < 3 ? s2b(2, k, z) : c2b(2, z); };
+        lapZ_off[2 * k] = push_z([&](int z) { return zb(z) + za(z); });
+        lapZ_off[2 * k + 1] = push_z([&](int z) { return zb(z) - za(z); });
     }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -630,12 +641,12 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         ctx->coef.dkapz = b0 + kap_off + nz;
         ctx->coef.dkz = b0 + kap_off + 2 * (size_t)nz;
         ctx->coef.uniform_xy = uxy ? 1 : 0;
-        for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lap_off + (size_t)set * nz;
-        ctx->coef.kxz = b0 + lap_off + 6 * (size_t)nz;
-        ctx->coef.kyz = b0 + lap_off + 7 * (size_t)nz;
-        ctx->coef.ocz1 = b0 + lap_off + 8 * (size_t)nz;
-        for (int t = 0; t < 5; t++) ctx->coef.condT[t] = b0 + lap_off + (size_t)(9 + t) * nz;
-        for (int t = 0; t < 8; t++) ctx->coef.lapZ[t] = b0 + lap_off + (size_t)(14 + t) * nz;
+        for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lapS_off[set];
+        ctx->coef.kxz = b0 + kxz_off;
+        ctx->coef.kyz = b0 + kyz_off;
+        ctx->coef.ocz1 = b0 + ocz1_off;
+        for (int t = 0; t < 5; t++) ctx->coef.condT[t] = b0 + condT_off[t];
+        for (int t = 0; t < 8; t++) ctx->coef.lapZ[t] = b0 + lapZ_off[t];
     }
     c.C13 = ctx->k.C13; c.C23 = ctx->k.C23; c.C43 = ctx->k.C43;
     c.hx = ctx->k.hx; c.h2x = ctx->k.h2x; c.hy = ctx->k.hy; c.h2y = ctx->k.h2y; c.hz = ctx->k.hz; c.h2z = ctx->k.h2z;
