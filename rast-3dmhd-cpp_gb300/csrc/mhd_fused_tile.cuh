@@ -243,10 +243,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             auto lapx = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, XP(q), XM(q), C0(q), sx[2 * k], sx[2 * k + 1]); };
             auto lapy = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, YP(q), YM(q), C0(q), sy[2 * k], sy[2 * k + 1]); };
             auto lapz = [&](double acc, int q, int k) { return acc_d2<true>(acc, ZP(q), ZM(q), C0(q), sz[2 * k], sz[2 * k + 1]); };
-            // uniform x / y: acc + sxb (px + mx) + syb (py + my) + (sza (pz - mz) + szb (pz + mz)) - c S,
-            // S = 2 (sxb + syb + szb) from the per-z table: one -2c product for the three axes
-            // the z part sza (pz - mz) + szb (pz + mz) as pz (szb + sza) + mz (szb - sza): szpm
-            // points at the per-z pair of tables
+            // uniform x / y: acc + sxb (px + mx) + syb (py + my) + pz (szb + sza) + mz (szb - sza) - c S,
+            // i.e. the scaled Laplacian with its z part sza (pz - mz) + szb (pz + mz) regrouped;
+            // szpm points at the per-z pair of tables (szb + sza, szb - sza), and S = 2 (sxb + syb
+            // + szb) comes from a per-z table: one -2c product for the three axes
             auto lap3 = [&](double acc, int q, double sxb, double syb, const double* const* szpm, double S) {
                 acc = fma(ZP(q), szpm[0][z], acc);
                 acc = fma(ZM(q), szpm[1][z], acc);
