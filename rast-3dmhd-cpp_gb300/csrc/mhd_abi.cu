@@ -641,6 +641,7 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         ctx->coef.dkapz = b0 + kap_off + nz;
         ctx->coef.dkz = b0 + kap_off + 2 * (size_t)nz;
         ctx->coef.uniform_xy = uxy ? 1 : 0;
+        ctx->coef.isotropic_xy = (uxy && c1(0, 1) == c1(1, 1)) ? 1 : 0;
         for (int set = 0; set < 6; set++) ctx->coef.lapS[set] = b0 + lapS_off[set];
         ctx->coef.kxz = b0 + kxz_off;
         ctx->coef.kyz = b0 + kyz_off;

@@ -91,6 +91,10 @@ struct Coefs {
     // uniform x and y grids: d2xxdx2 and d2yydy2 vanish and the x / y
     // coefficients are the same in every interior column
     int uniform_xy;
+    // with uniform_xy: the same first-derivative coefficient on x and y
+    // (cx1 = cy1, equal spacings), so the x and y advection and induction
+    // terms of a component can share one metric product
+    int isotropic_xy;
     // with uniform_xy, per z: S = 2 (sx + sy + sz) of the second-derivative
     // coefficients (the 'b' ones) of the Laplacians of u, v, w (viscous,
     // C43 on the x, y, z axis respectively), T (plain), B (resistive), and

@@ -33,14 +33,14 @@ constexpr bool kExtra = MHD_FUSED_XP != 0;
 using DefaultTile = Tile<MHD_FUSED_TILE_X, MHD_FUSED_TILE_Y>;
 constexpr int kMinBlocks = DefaultTile::kThreads >= 256 ? 2 : 3;
 
-template <class SW, bool UXY>
+template <class SW, bool UXY, bool ISO>
 __global__ void __launch_bounds__(DefaultTile::kThreads, kMinBlocks) k_substage(FusedArgs a) {
     extern __shared__ double ring[];
     const int lo = a.zhi > 0 ? a.zlo : 1;
     const int nz = (a.zhi > 0 ? a.zhi : a.g.nz - 1) - lo;
     const int zb = lo + (int)((long long)nz * blockIdx.z / gridDim.z);
     const int ze = lo + (int)((long long)nz * (blockIdx.z + 1) / gridDim.z);
-    substage_tile<SW, DefaultTile, UXY, kExtra>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
+    substage_tile<SW, DefaultTile, UXY, kExtra, ISO>(a, blockIdx.x, blockIdx.y, zb, ze, ring);
 }
 
 template <class SW>
@@ -68,29 +68,31 @@ int choose_chunks(long long tiles, int slots, int nPz) {
     return best;
 }
 
-template <class SW, bool UXY>
+template <class SW, bool UXY, bool ISO>
 int launch_t(const FusedArgs& a, cudaStream_t st) {
     using T = DefaultTile;
     const size_t smem = ring_bytes<SW, T>();
     static int slots = 0;
     if (!slots) {
-        cudaFuncSetAttribute(k_substage<SW, UXY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_substage<SW, UXY, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int dev = 0, sms = 0, per_sm = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substage<SW, UXY>, T::kThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substage<SW, UXY, ISO>, T::kThreads, smem);
         slots = sms * (per_sm > 0 ? per_sm : 1);
     }
     const int nbx = (a.g.nx - 2 + T::kTX - 1) / T::kTX, nby = (a.g.ny - 2 + T::kTY - 1) / T::kTY;
     const int planes = a.zhi > 0 ? a.zhi - a.zlo : a.g.nz - 2;
     const int chunks = choose_chunks((long long)nbx * nby, slots, planes);
-    k_substage<SW, UXY><<<dim3(nbx, nby, chunks), T::kThreads, smem, st>>>(a);
+    k_substage<SW, UXY, ISO><<<dim3(nbx, nby, chunks), T::kThreads, smem, st>>>(a);
     return (int)cudaGetLastError();
 }
 
 template <class SW>
 void launch_substage(const FusedArgs& a, cudaStream_t st, int* rc) {
-    *rc = a.k.uniform_xy ? launch_t<SW, true>(a, st) : launch_t<SW, false>(a, st);
+    // the instantiation with the optional temperature terms has no isotropic variant
+    if (!kExtra && a.k.uniform_xy && a.k.isotropic_xy) *rc = launch_t<SW, true, !kExtra>(a, st);
+    else *rc = a.k.uniform_xy ? launch_t<SW, true, false>(a, st) : launch_t<SW, false, false>(a, st);
 }
 
 template <class SW>

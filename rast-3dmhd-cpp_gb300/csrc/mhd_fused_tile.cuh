@@ -28,7 +28,8 @@
 //     product instead of one per axis, no (pz - mz) / (pz + mz); the
 //     conduction coefficient kappa(z) and the DKAPA dT/dz term are folded
 //     into the temperature's tables, and the cross-term factors are per-z
-//     tables too;
+//     tables too; with equal x and y spacings (cx1 = cy1) the x and y parts
+//     of each advection and induction component share one metric product;
 //   * with lShr (no temperature advection or heating) the velocity gradients
 //     feed only the induction terms, which are grouped per axis over raw
 //     differences with the metric factor applied once per group, and OBETA
@@ -171,8 +172,10 @@ __device__ __forceinline__ double acc_d2(double acc, double p, double m, double 
 
 // One tile (bx, by) of one instance, z planes [zb, ze) of the interior.
 // EXTRA: the instantiation with the optional temperature terms (the iTCon 2
-// plume heat sink, lRem); the others carry no code for them.
-template <class SW, class T, bool UXY, bool EXTRA = false>
+// plume heat sink, lRem); the others carry no code for them.  ISO (with UXY):
+// cx1 = cy1, the x and y parts of the advection and induction terms summed
+// before one metric product.
+template <class SW, class T, bool UXY, bool EXTRA = false, bool ISO = false>
 __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by, int zb, int ze, double* ring) {
     constexpr int NQ = nq<SW>();
     constexpr int kTX = T::kTX, kPX = T::kPX, kPlane = T::kPlane, kTY = T::kTY;
@@ -268,15 +271,29 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             // ---- pressure, gravity (3dmhdsub.h:266-272) and momentum advection
             // (3dmhdsub.h:279-289): F_i = -D_i P - D_j(RU_i u_j), + GRAV rho in z; the
             // diagonal terms difference P + RU_i u_i in one go
-            double fu = -cx1 * (fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P)));
-            double fv = -cy1 * (fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P)));
+            double fu, fv;
             double fw = fma(ro, c.GRAV, -cz1 * (fma(ZP(Q_RW), ZP(Q_W), ZP(Q_P)) - fma(ZM(Q_RW), ZM(Q_W), ZM(Q_P))));
-            fu = fma(-cy1, fma(YP(Q_RU), YP(Q_V), -YM(Q_RU) * YM(Q_V)), fu);
+            if constexpr (ISO) {
+                // cx1 = cy1: each component's x and y fluxes are summed before one metric product
+                double tu = fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P));
+                tu = fma(-YM(Q_RU), YM(Q_V), fma(YP(Q_RU), YP(Q_V), tu));
+                double tv = fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P));
+                tv = fma(-XM(Q_RV), XM(Q_U), fma(XP(Q_RV), XP(Q_U), tv));
+                double tw = fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U));
+                tw = fma(-YM(Q_RW), YM(Q_V), fma(YP(Q_RW), YP(Q_V), tw));
+                fu = -cx1 * tu;
+                fv = -cx1 * tv;
+                fw = fma(-cx1, tw, fw);
+            } else {
+                fu = -cx1 * (fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P)));
+                fv = -cy1 * (fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P)));
+                fu = fma(-cy1, fma(YP(Q_RU), YP(Q_V), -YM(Q_RU) * YM(Q_V)), fu);
+                fv = fma(-cx1, fma(XP(Q_RV), XP(Q_U), -XM(Q_RV) * XM(Q_U)), fv);
+                fw = fma(-cx1, fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U)), fw);
+                fw = fma(-cy1, fma(YP(Q_RW), YP(Q_V), -YM(Q_RW) * YM(Q_V)), fw);
+            }
             fu = fma(-cz1, fma(ZP(Q_RU), ZP(Q_W), -ZM(Q_RU) * ZM(Q_W)), fu);
-            fv = fma(-cx1, fma(XP(Q_RV), XP(Q_U), -XM(Q_RV) * XM(Q_U)), fv);
             fv = fma(-cz1, fma(ZP(Q_RV), ZP(Q_W), -ZM(Q_RV) * ZM(Q_W)), fv);
-            fw = fma(-cx1, fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U)), fw);
-            fw = fma(-cy1, fma(YP(Q_RW), YP(Q_V), -YM(Q_RW) * YM(Q_V)), fw);
 
             // ---- temperature: advection (3dmhdsub.h:293-296), conduction (:315-319)
             const double dTz = ZP(Q_TT) - ZM(Q_TT);
@@ -409,13 +426,24 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     const double dBXx = XP(Q_BX) - XM(Q_BX), dBXy = YP(Q_BX) - YM(Q_BX), dBXz = ZP(Q_BX) - ZM(Q_BX);
                     const double dBYx = XP(Q_BY) - XM(Q_BY), dBYy = YP(Q_BY) - YM(Q_BY), dBYz = ZP(Q_BY) - ZM(Q_BY);
                     const double dBZx = XP(Q_BZ) - XM(Q_BZ), dBZy = YP(Q_BZ) - YM(Q_BZ), dBZz = ZP(Q_BZ) - ZM(Q_BZ);
-                    const double cxu = cx1 * u, cyv = cy1 * v, czw = cz1 * w;
-                    w1 = fma(-cxu, dBXx, fma(cy1, fma(by, dUy, fma(-v, dBXy, -bx * dVy)),
-                                             cz1 * fma(bz, dUz, fma(-w, dBXz, -bx * dWz))));
-                    w2 = fma(cx1, fma(bx, dVx, fma(-u, dBYx, -by * dUx)),
-                             fma(-cyv, dBYy, cz1 * fma(bz, dVz, fma(-w, dBYz, -by * dWz))));
-                    w3 = fma(cx1, fma(bx, dWx, fma(-u, dBZx, -bz * dUx)),
-                             fma(cy1, fma(by, dWy, fma(-v, dBZy, -bz * dVy)), -czw * dBZz));
+                    const double czw = cz1 * w;
+                    if constexpr (ISO) {
+                        // cx1 = cy1: each component's x and y terms share one metric product
+                        w1 = fma(cx1, fma(-u, dBXx, fma(by, dUy, fma(-v, dBXy, -bx * dVy))),
+                                 cz1 * fma(bz, dUz, fma(-w, dBXz, -bx * dWz)));
+                        w2 = fma(cx1, fma(-v, dBYy, fma(bx, dVx, fma(-u, dBYx, -by * dUx))),
+                                 cz1 * fma(bz, dVz, fma(-w, dBYz, -by * dWz)));
+                        w3 = fma(cx1, fma(by, dWy, fma(-v, dBZy, fma(-bz, dVy, fma(bx, dWx, fma(-u, dBZx, -bz * dUx))))),
+                                 -czw * dBZz);
+                    } else {
+                        const double cxu = cx1 * u, cyv = cy1 * v;
+                        w1 = fma(-cxu, dBXx, fma(cy1, fma(by, dUy, fma(-v, dBXy, -bx * dVy)),
+                                                 cz1 * fma(bz, dUz, fma(-w, dBXz, -bx * dWz))));
+                        w2 = fma(cx1, fma(bx, dVx, fma(-u, dBYx, -by * dUx)),
+                                 fma(-cyv, dBYy, cz1 * fma(bz, dVz, fma(-w, dBYz, -by * dWz))));
+                        w3 = fma(cx1, fma(bx, dWx, fma(-u, dBZx, -bz * dUx)),
+                                 fma(cy1, fma(by, dWy, fma(-v, dBZy, -bz * dVy)), -czw * dBZz));
+                    }
                     const double ocz1 = K.ocz1[z];  // OBETA cz1
                     jz = fma(ocx1, dBYx, -ocy1 * dBXy);
                     jy = fma(ocz1, dBXz, -ocx1 * dBZx);

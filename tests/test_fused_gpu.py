@@ -42,6 +42,19 @@ def test_one_step_all_switch_sets(mag, rot, shr):
         assert e <= TOL_ONE_STEP, (k, e)
 
 
+@pytest.mark.parametrize("mag,rot,shr", SWITCHES)
+def test_one_step_isotropic_xy(mag, rot, shr):
+    """Equal x and y spacings (nPx = nPy, xMax = yMax; the cases above have
+    nPx != nPy) run the isotropic instantiation, in which the x and y parts
+    of the advection and induction terms share one metric product."""
+    base = small_cases()["mhd_fixedT"]
+    case = base.replace(lMag=mag, lRot=rot, lShr=shr, ANG=0.3, nPx=16, nPy=16, nPz=10)
+    got, o = run_pair(case, 1)
+    for k in STATE_FIELDS[:case.nfields]:
+        e = rel_err(got[k], o.arr[k])
+        assert e <= TOL_ONE_STEP, (k, e)
+
+
 @pytest.mark.parametrize("name", sorted(small_cases()))
 def test_one_step_boundary_variants(name):
     case = small_cases()[name]
