@@ -1,8 +1,9 @@
 // mhd_fused_batch.cu -- the fused FP64 substage over a ragged batch of
 // instances: persistent CTAs take (instance, tile x, tile y, z range) work
 // items from a counter until none are left, so instances of different sizes
-// share one launch.  Built twice: MHD_BATCH_UXY = 1 for uniform x/y grids,
-// 0 for stretched ones; the tile shapes are the autotuner's candidates.
+// share one launch.  Built twice: MHD_BATCH_UXY = 1 for uniform x/y grids
+// (with the isotropic variant chosen per work item), 0 for stretched ones;
+// the tile shapes are the autotuner's candidates.
 #include "mhd_fused_tile.cuh"
 
 #ifndef MHD_BATCH_UXY
@@ -32,7 +33,11 @@ __global__ void __launch_bounds__(T::kThreads) k_substage_batch(const FusedArgs*
         __syncthreads();
         if (t >= nitems) break;
         const int4 it = items[t];
-        substage_tile<SW, T, kUXY>(args[it.x], it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
+        const FusedArgs& a = args[it.x];
+        // each instance runs the variant it runs alone (isotropic or not), so
+        // a batch reproduces its instances' single-instance results bit for bit
+        if (kUXY && a.k.isotropic_xy) substage_tile<SW, T, kUXY, false, kUXY>(a, it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
+        else substage_tile<SW, T, kUXY>(a, it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
         __syncthreads();
     }
 }
