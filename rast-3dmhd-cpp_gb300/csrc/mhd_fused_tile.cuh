@@ -3,8 +3,9 @@
 // A CTA owns a TX x TY tile of (x, y) columns and marches down a range of z
 // planes.  Three z-planes of the tile plus a one-cell halo live in a
 // shared-memory ring; when plane z+2 is loaded its derived quantities (1/rho,
-// the velocities u = RU/rho, v, w and the pressure p = rho*T) are computed
-// once per point, so every stencil reads them instead of recomputing them.
+// the velocities u = RU/rho, v, w and the diagonal momentum fluxes
+// p + RU u, p + RV v, p + RW w with the pressure p = rho*T) are computed once
+// per point, so every stencil reads them instead of recomputing them.
 // One thread per column then evaluates the whole right-hand side of fluxes()
 // (3dmhdsub.h:194-696) for cell (z, y, x), applies the RK update of
 // step_block_GAM (3dmhdsub.h:181-192), forms the next substage's register
@@ -35,8 +36,8 @@
 //     differences with the metric factor applied once per group, and OBETA
 //     rides in the current density;
 //   * the pressure is differenced together with the diagonal momentum flux
-//     (P + RU_i u_i), and the temperature terms proportional to 1/rho are
-//     summed before one multiply;
+//     (P + RU_i u_i, formed once per point, not once per neighbour), and the
+//     temperature terms proportional to 1/rho are summed before one multiply;
 //   * load_plane forms per point the z differences of u, v, w and the x
 //     differences of u, v (difference arrays after the ring), from which the
 //     viscous mixed derivatives are one subtraction of two neighbours' values;
@@ -67,8 +68,10 @@ struct Tile {
     static constexpr int kPlane = kPX * kPY;
 };
 
-// quantities held per plane point
-enum Q { Q_RU = 0, Q_RV, Q_RW, Q_TT, Q_RO, Q_RI, Q_U, Q_V, Q_W, Q_P, Q_BX, Q_BY, Q_BZ, Q_N };
+// quantities held per plane point; Q_PX, Q_PY, Q_PZ are the diagonal momentum
+// fluxes P + RU u, P + RV v, P + RW w (P = rho T), which both neighbours of a
+// point difference
+enum Q { Q_RU = 0, Q_RV, Q_RW, Q_TT, Q_RO, Q_RI, Q_U, Q_V, Q_W, Q_PX, Q_PY, Q_PZ, Q_BX, Q_BY, Q_BZ, Q_N };
 
 template <class SW>
 constexpr int nq() {
@@ -127,7 +130,10 @@ __device__ __forceinline__ void load_plane(const FusedArgs& a, double* ring, int
         base[Q_U * kPlane + k] = uu;
         base[Q_V * kPlane + k] = vv;
         base[Q_W * kPlane + k] = ww;
-        base[Q_P * kPlane + k] = ro * tt;
+        const double p = __dmul_rn(ro, tt);
+        base[Q_PX * kPlane + k] = fma(ru, uu, p);
+        base[Q_PY * kPlane + k] = fma(rv, vv, p);
+        base[Q_PZ * kPlane + k] = fma(rw, ww, p);
         if (diffs) {
             const double* Pm2 = ring + (size_t)((slot + 1) % 3) * NQ * kPlane;  // plane z-2
             const double* Pm1 = ring + (size_t)((slot + 2) % 3) * NQ * kPlane;  // plane z-1
@@ -270,14 +276,14 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
 
             // ---- pressure, gravity (3dmhdsub.h:266-272) and momentum advection
             // (3dmhdsub.h:279-289): F_i = -D_i P - D_j(RU_i u_j), + GRAV rho in z; the
-            // diagonal terms difference P + RU_i u_i in one go
+            // diagonal terms difference P + RU_i u_i, formed once per point by load_plane
             double fu, fv;
-            double fw = fma(ro, c.GRAV, -cz1 * (fma(ZP(Q_RW), ZP(Q_W), ZP(Q_P)) - fma(ZM(Q_RW), ZM(Q_W), ZM(Q_P))));
+            double fw = fma(ro, c.GRAV, -cz1 * (ZP(Q_PZ) - ZM(Q_PZ)));
             if constexpr (ISO) {
                 // cx1 = cy1: each component's x and y fluxes are summed before one metric product
-                double tu = fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P));
+                double tu = XP(Q_PX) - XM(Q_PX);
                 tu = fma(-YM(Q_RU), YM(Q_V), fma(YP(Q_RU), YP(Q_V), tu));
-                double tv = fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P));
+                double tv = YP(Q_PY) - YM(Q_PY);
                 tv = fma(-XM(Q_RV), XM(Q_U), fma(XP(Q_RV), XP(Q_U), tv));
                 double tw = fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U));
                 tw = fma(-YM(Q_RW), YM(Q_V), fma(YP(Q_RW), YP(Q_V), tw));
@@ -285,8 +291,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                 fv = -cx1 * tv;
                 fw = fma(-cx1, tw, fw);
             } else {
-                fu = -cx1 * (fma(XP(Q_RU), XP(Q_U), XP(Q_P)) - fma(XM(Q_RU), XM(Q_U), XM(Q_P)));
-                fv = -cy1 * (fma(YP(Q_RV), YP(Q_V), YP(Q_P)) - fma(YM(Q_RV), YM(Q_V), YM(Q_P)));
+                fu = -cx1 * (XP(Q_PX) - XM(Q_PX));
+                fv = -cy1 * (YP(Q_PY) - YM(Q_PY));
                 fu = fma(-cy1, fma(YP(Q_RU), YP(Q_V), -YM(Q_RU) * YM(Q_V)), fu);
                 fv = fma(-cx1, fma(XP(Q_RV), XP(Q_U), -XM(Q_RV) * XM(Q_U)), fv);
                 fw = fma(-cx1, fma(XP(Q_RW), XP(Q_U), -XM(Q_RW) * XM(Q_U)), fw);
