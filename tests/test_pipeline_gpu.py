@@ -41,10 +41,12 @@ def _reference_steps(case, st, n):
     return out
 
 
-@pytest.mark.parametrize("mag,shr,npz", [(True, True, 100), (True, False, 96), (False, True, 130), (True, True, 40)])
+# nPy = 48: the isotropic instantiation (equal x and y spacings), 40: the uniform one
+@pytest.mark.parametrize("mag,shr,npz,npy", [(True, True, 100, 40), (True, False, 96, 40), (False, True, 130, 40),
+                                             (True, True, 40, 40), (True, True, 100, 48)])
 @pytest.mark.parametrize("pinned", [True, False])
-def test_step_host_equals_device_step(mag, shr, npz, pinned):
-    case = Case(nPx=48, nPy=40, nPz=npz, lMag=mag, lRot=True, lShr=shr, seed=21, name="pipe")
+def test_step_host_equals_device_step(mag, shr, npz, npy, pinned):
+    case = Case(nPx=48, nPy=npy, nPz=npz, lMag=mag, lRot=True, lShr=shr, seed=21, name="pipe")
     st = initial_state(case)
     # ghosts as communicate() leaves them, so both paths start from the same arrays
     s0 = Simulation(case)
