@@ -253,6 +253,14 @@ int mhd_steps_cfl(mhd_ctx* ctx, int n, mhd_diag* out);
  * mhd_sync).  Replaces the transfers around step() of a host-resident driver;
  * the reference has no counterpart (its state never leaves the host). */
 int mhd_step_host(mhd_ctx* ctx, const double* in, double* out, double dt);
+/* n fixed-dt steps through host memory: the same as mhd_step_host(ctx, in,
+ * out, dt) followed by n-1 calls mhd_step_host(ctx, out, out, dt) (every step
+ * uploads its input and downloads its result; bit-identical), but the steps
+ * are enqueued back to back, so each step's first slabs overlap the previous
+ * step's last slabs and downloads instead of waiting for them.  Blocks until
+ * `out` holds the last result (out = NULL: no downloads, steps 1..n-1 start
+ * from the device state, and the call does not block). */
+int mhd_steps_host(mhd_ctx* ctx, int n, const double* in, double* out, double dt);
 /* Mass, energy, max|div B| and sanity flags of the current state (blocks). */
 int mhd_diagnostics(mhd_ctx* ctx, mhd_diag* out);
 int mhd_sync(mhd_ctx* ctx);

@@ -115,6 +115,7 @@ SIGNATURES = {
     "mhd_steps": [C.c_void_p, C.c_int, C.c_double],
     "mhd_steps_cfl": [C.c_void_p, C.c_int, C.POINTER(MhdDiag)],
     "mhd_step_host": [C.c_void_p, _DP, _DP, C.c_double],
+    "mhd_steps_host": [C.c_void_p, C.c_int, _DP, _DP, C.c_double],
     "mhd_set_plume": [C.c_void_p, C.POINTER(MhdPlume)],
     "mhd_selftest_convert": [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "mhd_static_state": [C.POINTER(MhdParams), C.POINTER(MhdStaticParams), _DP],

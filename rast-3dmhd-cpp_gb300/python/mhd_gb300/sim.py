@@ -188,12 +188,22 @@ class Simulation:
         """One fused step from a host state to a host state (mhd_step_host);
         host_in / host_out are float64 arrays of nf x nz x ny x nx (or None),
         the upload / step / download overlapped slab by slab."""
-        def ptr(a):
-            if a is None:
-                return None
-            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.case.nfields * self.ncell_all
-            return _dp(a)
-        self._ck(self.L.mhd_step_host(self.ctx, ptr(host_in), ptr(host_out), self.case.dt if dt is None else dt))
+        self._ck(self.L.mhd_step_host(self.ctx, self._host_ptr(host_in), self._host_ptr(host_out),
+                                      self.case.dt if dt is None else dt))
+
+    def steps_host(self, n: int, host_in, host_out, dt: float | None = None) -> None:
+        """n fused steps through host memory (mhd_steps_host): step 0 reads
+        host_in, every later step the previous result in host_out, and every
+        step writes host_out; the steps are enqueued back to back."""
+        self._ck(self.L.mhd_steps_host(self.ctx, n, self._host_ptr(host_in), self._host_ptr(host_out),
+                                       self.case.dt if dt is None else dt))
+
+    def _host_ptr(self, a):
+        """A float64 state array of nf x nz x ny x nx as a double pointer (None: NULL)."""
+        if a is None:
+            return None
+        assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.case.nfields * self.ncell_all
+        return _dp(a)
 
     @property
     def ncell_all(self) -> int:

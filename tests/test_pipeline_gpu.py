@@ -92,3 +92,54 @@ def test_step_host_separate_buffers_and_device_input():
     sim.step_host(None, out)                  # device state -> host
     sim.close()
     assert np.array_equal(out.reshape(want2.shape), want2)
+
+
+@pytest.mark.parametrize("mag,shr,npz,npy", [(True, True, 100, 48), (True, False, 130, 40), (False, True, 96, 40)])
+def test_steps_host_chained_equals_device_steps(mag, shr, npz, npy):
+    """mhd_steps_host: n host-to-host steps enqueued back to back (each step's
+    upload of slab j waits only for the previous step's download of slab j+1)
+    give the device steps bit for bit; the input buffer is left alone."""
+    case = Case(nPx=48, nPy=npy, nPz=npz, lMag=mag, lRot=True, lShr=shr, seed=23, name="chain")
+    st = initial_state(case)
+    s0 = Simulation(case)
+    s0.upload_state(st)
+    s0.communicate()
+    st = s0.download_state()
+    s0.close()
+    want = _reference_steps(case, st, 4)
+    flat = _flat(case, st)
+    src = flat.ravel().copy()
+    buf = Pinned(flat.size)
+    sim = Simulation(case)
+    sim.steps_host(4, src, buf.a)             # separate in / out, pinned out
+    got = buf.a.reshape(flat.shape).copy()
+    assert np.array_equal(src, flat.ravel())
+    assert sim.diagnostics()["nit"] == 4
+    # aliased in / out on pageable memory, continuing from the pinned result
+    arr = got.ravel().copy()
+    sim.steps_host(2, arr, arr)
+    sim.close()
+    buf.free()
+    for f, k in enumerate(STATE_FIELDS[:case.nfields]):
+        assert np.array_equal(got[f], want[f]), k
+    want6 = _reference_steps(case, st, 6)
+    assert np.array_equal(arr.reshape(flat.shape), want6)
+
+
+def test_steps_host_without_downloads_then_device_state():
+    """out = NULL: step 0 uploads, later steps start from the device state
+    (each substage 1 of slab j waits for the previous substage 3 of slab j+1)."""
+    case = Case(nPx=40, nPy=40, nPz=128, lMag=True, lShr=True, seed=24, name="chain2")
+    st = initial_state(case)
+    s0 = Simulation(case)
+    s0.upload_state(st)
+    s0.communicate()
+    st = s0.download_state()
+    s0.close()
+    want = _reference_steps(case, st, 3)
+    sim = Simulation(case)
+    sim.steps_host(3, _flat(case, st).ravel(), None)
+    sim.sync()
+    got = _flat(case, sim.download_state())
+    sim.close()
+    assert np.array_equal(got, want)
