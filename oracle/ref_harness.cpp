@@ -134,8 +134,8 @@ int main(int argc, char** argv) {
     InHeader h;
     memcpy(&h, raw.data(), sizeof(h));
     if (h.magic != kMagic) die("bad magic");
-    if (h.gx != nPx || h.gy != nPy || h.gz != nPz) die("grid size of the input does not match this build");
-    if (h.mag != (lMag ? 1 : 0)) die("lMag of the input does not match this build");
+    if (h.gx != nPx || h.gy != nPy || h.gz != nPz) die("grid size of the input does not match the compiled parameters");
+    if (h.mag != (lMag ? 1 : 0)) die("lMag of the input does not match the compiled parameters");
 
     const int gnx = nPx + ix, gny = nPy + iy, gnz = nPz + iz;
     const size_t nglob = (size_t)gnz * gny * gnx;
