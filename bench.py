@@ -372,7 +372,7 @@ def run_ours(args, dist: Dist) -> None:
 # keyed by (lMag, lRot, lShr): ncu's sm__inst_executed_pipe_fp64 share x the
 # 2/clk/SM pipe rate x elapsed cycles / cells, from the 256x256x128 capture in
 # profiles/k_substage_fp64_config1physics_256x256x128.md.
-FP64_INST_PER_CELL_SUBSTAGE: dict = {(True, True, True): 201.4}
+FP64_INST_PER_CELL_SUBSTAGE: dict = {(True, True, True): 200.5}
 # DRAM traffic over algorithmic bytes of one k_substage launch, measured by ncu
 # at 256x256x128 (2.274 GB / 2.282 GB); applied to the full-size average launch.
 TRAFFIC_OVER_ALGORITHMIC = {(True, True, True): 2.274 / 2.282}
