@@ -267,6 +267,18 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             const double ro = C0(Q_RO), ri = C0(Q_RI), tt = C0(Q_TT);
             const double u = C0(Q_U), v = C0(Q_V), w = C0(Q_W);
             const long long i = (long long)z * g.sz + (long long)y * g.sy + x;
+            // the RK register (read by substages 2 and 3) and FT of this column's
+            // next plane into L2, so the next iteration's epilogue does not wait
+            // on DRAM for them
+            if (z + 1 < ze) {
+                const long long inx = i + g.sz;
+                if (a.substage != 0) {
+#pragma unroll
+                    for (int f = 0; f < 8; f++)
+                        if (f < (SW::lMag ? 8 : 5)) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Z.p[f] + inx));
+                }
+                if constexpr (SW::lShr) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.FT + inx));
+            }
 
             // ---- continuity (3dmhdsub.h:204-227), one-sided dRW/dz on the walls
             double rwz = ZP(Q_RW) - ZM(Q_RW);
