@@ -34,6 +34,8 @@ import numpy as np
 from .case import Case, STATE_FIELDS, initial_state
 from .sim import Batch, Simulation
 
+DEFAULT_TILE = 2  # the 16x8 batch tile, the shape of the single-instance kernel
+
 
 @dataclass
 class Request:
@@ -104,8 +106,10 @@ class Server:
 
     quantum: at most this many steps are queued per resident simulation
     between scheduling decisions (admissions and completions happen between
-    quanta).  tile: batch tile shape (None = autotune once, then keep it, so
-    every batch of the run uses the same kernel instance)."""
+    quanta).  tile: batch tile shape (None = the 16x8 tile until an FP64
+    batch holds at least a quarter of target_cells, then the autotuner's
+    choice on that batch, kept for the rest of the run: a tuning on the first,
+    often tiny, batch would fix a shape that suits a handful of small grids)."""
 
     def __init__(self, hbm_budget_bytes: int, quantum: int = 25, tile: int | None = None,
                  keep_results: bool = False, device_init: bool = True, policy: str = "srpt",
@@ -118,6 +122,7 @@ class Server:
         self.budget = int(hbm_budget_bytes)
         self.quantum = int(quantum)
         self.tile = tile
+        self.tuned = tile is not None
         self.keep_results = keep_results
         self.device_init = device_init
         self.used = 0
@@ -175,9 +180,10 @@ class Server:
             if key not in self.batches:
                 b = Batch([self.resident[r].sim for r in rids])
                 if key[0] == "fp64":
-                    if self.tile is None:
+                    if not self.tuned and sum(self.resident[r].sim.case.cells for r in rids) >= self.target_cells // 4:
                         self.tile, _ = b.autotune(report=False)
-                    b.set_tile(self.tile)
+                        self.tuned = True
+                    b.set_tile(self.tile if self.tile is not None else DEFAULT_TILE)
                 else:
                     b.set_tile(0)
                 self.batches[key] = b
@@ -259,7 +265,8 @@ class Server:
         return {"requests": len(reqs), "policy": self.policy, "wall_s": wall, "cell_steps": self.cell_steps,
                 "value": self.cell_steps / wall if wall > 0 else None,
                 "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
-                "max_resident": self.max_resident, "batch_rebuilds": self.batch_rebuilds, "tile": self.tile}
+                "max_resident": self.max_resident, "batch_rebuilds": self.batch_rebuilds,
+                "tile": self.tile if self.tile is not None else DEFAULT_TILE}
 
 
 def run_serial(requests: list, device_init: bool = True) -> dict:

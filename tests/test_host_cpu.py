@@ -103,8 +103,33 @@ def test_scheduler_admits_under_budget_and_completes_every_request(fake_backend)
     assert FakeSim.live == 0 and srv.used == 0
     assert all(r.result["steps"] == r.steps for r in reqs)          # each ran exactly its step count
     assert all(r.t_done >= r.t_admit >= r.arrival for r in reqs)
-    assert st["max_resident"] >= 2 and st["tile"] == 1
+    # no batch reached a quarter of the 64 M-cell target: the default tile, never tuned
+    assert st["max_resident"] >= 2 and st["tile"] == serve.DEFAULT_TILE
     assert st["tts_p99_s"] >= st["tts_p50_s"] > 0
+
+
+def test_server_tunes_the_tile_once_on_a_representative_batch(fake_backend, monkeypatch):
+    tuned, tiles = [], []
+
+    class CountingBatch(FakeBatch):
+        def autotune(self, report=True):
+            tuned.append(len(self.sims))
+            tiles.append((len(self.sims), "tuned"))
+            return super().autotune(report)
+
+        def set_tile(self, t):
+            tiles.append((len(self.sims), t))
+            super().set_tile(t)
+    monkeypatch.setattr(serve, "Batch", CountingBatch)
+    reqs = poisson_requests(24, rate=1000.0, seed=5, grid_min=(32, 32, 16), grid_max=(32, 32, 16), steps=(20, 40),
+                            fp32_fraction=0.0)
+    cells = reqs[0].case.cells
+    srv = Server(1 << 40, quantum=5, target_cells=16 * cells)        # tuned from 4 instances on
+    st = srv.run(reqs, realtime=False)
+    assert len(tuned) == 1 and tuned[0] >= 4
+    k = tiles.index((tuned[0], "tuned"))
+    assert k > 0 and all(t == serve.DEFAULT_TILE and n < 4 for n, t in tiles[:k])   # small batches first
+    assert all(t == 1 for n, t in tiles[k + 1:]) and st["tile"] == 1                # the tuned shape from then on
 
 
 def test_srpt_admits_least_work_first_and_caps_resident_cells(fake_backend):
