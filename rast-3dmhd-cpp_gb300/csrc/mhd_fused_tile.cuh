@@ -33,8 +33,9 @@
 //     of each advection and induction component share one metric product;
 //   * with lShr (no temperature advection or heating) the velocity gradients
 //     feed only the induction terms, which are grouped per axis over raw
-//     differences with the metric factor applied once per group, and OBETA
-//     rides in the current density;
+//     differences with the metric factor applied once per group; without
+//     lShr the B differences stay raw and the metric factors ride in u cx1,
+//     v cy1, w cz1; OBETA rides in the current density;
 //   * the pressure is differenced together with the diagonal momentum flux
 //     (P + RU_i u_i, formed once per point, not once per neighbour), and the
 //     temperature terms proportional to 1/rho are summed before one multiply;
@@ -214,9 +215,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
     const double zdt = a.dtp ? a.zet * a.dtp[0] : a.zdt;
     const bool halted = a.dtp && a.dtp[3] != 0.0;
     const double ocvore = c.OCV * c.ORE;
-    const double ohm = c.OBETA * c.ORM * c.OCV;
-    // with lShr the current density carries OBETA (j' = OBETA j): the Lorentz force
-    // is B x j' and the Ohmic heating (ORM OCV / OBETA) |j'|^2
+    // the current density carries OBETA (j' = OBETA j): the Lorentz force is
+    // B x j' and the Ohmic heating (ORM OCV / OBETA) |j'|^2
     const double ocx1 = c.OBETA * cx1, ocy1 = c.OBETA * cy1;
     const double ohm2 = c.OBETA != 0.0 ? c.ORM * c.OCV / c.OBETA : 0.0;
 
@@ -247,7 +247,6 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             for (int k = 0; k < 6; k++) sz[k] = K.s2[2][k][z];
             auto Dx = [&](int q) { return (XP(q) - XM(q)) * cx1; };
             auto Dy = [&](int q) { return (YP(q) - YM(q)) * cy1; };
-            auto Dz = [&](int q) { return (ZP(q) - ZM(q)) * cz1; };
             // acc + s * (D2x + D2y + D2z) q with scale pair k (0: ORE, 1: ORE*C43, 2: ORM)
             auto lapx = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, XP(q), XM(q), C0(q), sx[2 * k], sx[2 * k + 1]); };
             auto lapy = [&](double acc, int q, int k) { return acc_d2<!UXY>(acc, YP(q), YM(q), C0(q), sy[2 * k], sy[2 * k + 1]); };
@@ -477,18 +476,22 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                         const long long j = i - 2 * g.sz;
                         wzm = (a.U.p[S_RW][j] / a.U.p[S_RO][j] - 4.0 * ZM(Q_W)) * cz1;
                     }
-                    const double bxx = Dx(Q_BX), bxy = Dy(Q_BX), bxz = Dz(Q_BX);
-                    const double byx = Dx(Q_BY), byy = Dy(Q_BY), byz = Dz(Q_BY);
-                    const double bzx = Dx(Q_BZ), bzy = Dy(Q_BZ), bzz = Dz(Q_BZ);
+                    // raw B differences: the metric factor rides in u cx1, v cy1, w cz1
+                    // for the advective terms and in OBETA c for the current density
+                    const double dBXx = XP(Q_BX) - XM(Q_BX), dBXy = YP(Q_BX) - YM(Q_BX), dBXz = ZP(Q_BX) - ZM(Q_BX);
+                    const double dBYx = XP(Q_BY) - XM(Q_BY), dBYy = YP(Q_BY) - YM(Q_BY), dBYz = ZP(Q_BY) - ZM(Q_BY);
+                    const double dBZx = XP(Q_BZ) - XM(Q_BZ), dBZy = YP(Q_BZ) - YM(Q_BZ), dBZz = ZP(Q_BZ) - ZM(Q_BZ);
+                    const double cxu = cx1 * u, cyv = cy1 * v, czw = cz1 * w;
                     w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
-                    w1 = fma(-u, bxx, fma(-v, bxy, fma(-w, bxz, w1)));
+                    w1 = fma(-cxu, dBXx, fma(-cyv, dBXy, fma(-czw, dBXz, w1)));
                     w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
-                    w2 = fma(-u, byx, fma(-v, byy, fma(-w, byz, w2)));
+                    w2 = fma(-cxu, dBYx, fma(-cyv, dBYy, fma(-czw, dBYz, w2)));
                     w3 = fma(bx, wx, fma(by, wy, -bz * (ux + vy)));
-                    w3 = fma(-u, bzx, fma(-v, bzy, fma(-w, bzz, w3)));
-                    jz = byx - bxy;
-                    jy = bxz - bzx;
-                    jx = bzy - byz;
+                    w3 = fma(-cxu, dBZx, fma(-cyv, dBZy, fma(-czw, dBZz, w3)));
+                    const double ocz1 = K.ocz1[z];  // OBETA cz1
+                    jz = fma(ocx1, dBYx, -ocy1 * dBXy);
+                    jy = fma(ocz1, dBXz, -ocx1 * dBZx);
+                    jx = fma(ocy1, dBZy, -ocz1 * dBYz);
                 }
                 const bool wall = (z == zl || z == zr - 1);
                 if constexpr (UXY) {
@@ -521,17 +524,10 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     w1 += sg * (-3.0 * bx + 4.0 * X1 - X2) * d2 + (2.0 * bx - 5.0 * X1 + 4.0 * X2 - X3) * d1;
                     w2 += sg * (-3.0 * by + 4.0 * Y1 - Y2) * d2 + (2.0 * by - 5.0 * Y1 + 4.0 * Y2 - Y3) * d1;
                 }
-                if constexpr (SW::lShr) {
-                    fu = fma(bz, jy, fma(-by, jz, fu));
-                    fv = fma(bx, jz, fma(-bz, jx, fv));
-                    fw = fma(by, jx, fma(-bx, jy, fw));
-                    qr = fma(ohm2, fma(jx, jx, fma(jy, jy, jz * jz)), qr);
-                } else {
-                    fu = fma(c.OBETA, fma(bz, jy, -by * jz), fu);
-                    fv = fma(c.OBETA, fma(bx, jz, -bz * jx), fv);
-                    fw = fma(c.OBETA, fma(by, jx, -bx * jy), fw);
-                    qr = fma(ohm, fma(jx, jx, fma(jy, jy, jz * jz)), qr);
-                }
+                fu = fma(bz, jy, fma(-by, jz, fu));
+                fv = fma(bx, jz, fma(-bz, jx, fv));
+                fw = fma(by, jx, fma(-bx, jy, fw));
+                qr = fma(ohm2, fma(jx, jx, fma(jy, jy, jz * jz)), qr);
             }
 
             ft = fma(ri, qr, ft);
