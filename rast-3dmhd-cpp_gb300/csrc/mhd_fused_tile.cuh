@@ -317,8 +317,14 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
             const double Tz = dTz * cz1;  // without lShr only (advection)
             double ft;
             double qr = 0.0;  // the temperature terms proportional to 1/rho, applied once at the end
+            // the velocities with their axis' metric factor (the T advection here
+            // and the advective induction terms below)
+            double cxu = 0.0, cyv = 0.0, czw = 0.0;
             if constexpr (!SW::lShr) {
-                ft = -fma(u, Dx(Q_TT), fma(v, Dy(Q_TT), w * Tz));
+                cxu = cx1 * u;
+                cyv = cy1 * v;
+                czw = cz1 * w;
+                ft = -fma(cxu, XP(Q_TT) - XM(Q_TT), fma(cyv, YP(Q_TT) - YM(Q_TT), czw * dTz));
             } else {
                 ft = a.FT[i];  // the reference never re-initialises FT with lShr
             }
@@ -443,7 +449,7 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     const double dBXx = XP(Q_BX) - XM(Q_BX), dBXy = YP(Q_BX) - YM(Q_BX), dBXz = ZP(Q_BX) - ZM(Q_BX);
                     const double dBYx = XP(Q_BY) - XM(Q_BY), dBYy = YP(Q_BY) - YM(Q_BY), dBYz = ZP(Q_BY) - ZM(Q_BY);
                     const double dBZx = XP(Q_BZ) - XM(Q_BZ), dBZy = YP(Q_BZ) - YM(Q_BZ), dBZz = ZP(Q_BZ) - ZM(Q_BZ);
-                    const double czw = cz1 * w;
+                    czw = cz1 * w;
                     if constexpr (ISO) {
                         // cx1 = cy1: each component's x and y terms share one metric product
                         w1 = fma(cx1, fma(-u, dBXx, fma(by, dUy, fma(-v, dBXy, -bx * dVy))),
@@ -453,7 +459,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                         w3 = fma(cx1, fma(by, dWy, fma(-v, dBZy, fma(-bz, dVy, fma(bx, dWx, fma(-u, dBZx, -bz * dUx))))),
                                  -czw * dBZz);
                     } else {
-                        const double cxu = cx1 * u, cyv = cy1 * v;
+                        cxu = cx1 * u;
+                        cyv = cy1 * v;
                         w1 = fma(-cxu, dBXx, fma(cy1, fma(by, dUy, fma(-v, dBXy, -bx * dVy)),
                                                  cz1 * fma(bz, dUz, fma(-w, dBXz, -bx * dWz))));
                         w2 = fma(cx1, fma(bx, dVx, fma(-u, dBYx, -by * dUx)),
@@ -481,7 +488,6 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     const double dBXx = XP(Q_BX) - XM(Q_BX), dBXy = YP(Q_BX) - YM(Q_BX), dBXz = ZP(Q_BX) - ZM(Q_BX);
                     const double dBYx = XP(Q_BY) - XM(Q_BY), dBYy = YP(Q_BY) - YM(Q_BY), dBYz = ZP(Q_BY) - ZM(Q_BY);
                     const double dBZx = XP(Q_BZ) - XM(Q_BZ), dBZy = YP(Q_BZ) - YM(Q_BZ), dBZz = ZP(Q_BZ) - ZM(Q_BZ);
-                    const double cxu = cx1 * u, cyv = cy1 * v, czw = cz1 * w;
                     w1 = fma(by, uy, fma(bz, uz, -bx * (vy + wzm)));
                     w1 = fma(-cxu, dBXx, fma(-cyv, dBXy, fma(-czw, dBXz, w1)));
                     w2 = fma(bx, vx, fma(bz, vz, -by * (ux + wzm)));
