@@ -314,7 +314,6 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
 
             // ---- temperature: advection (3dmhdsub.h:293-296), conduction (:315-319)
             const double dTz = ZP(Q_TT) - ZM(Q_TT);
-            const double Tz = dTz * cz1;  // without lShr only (advection)
             double ft;
             double qr = 0.0;  // the temperature terms proportional to 1/rho, applied once at the end
             // the velocities with their axis' metric factor (the T advection here
@@ -350,10 +349,8 @@ __device__ __forceinline__ void substage_tile(const FusedArgs& a, int bx, int by
                     q = fma(XP(Q_TT) + XM(Q_TT), K.condT[0][z], q);
                     q = fma(YP(Q_TT) + YM(Q_TT), K.condT[1][z], q);
                     qr = fma(-C0(Q_TT), K.condT[4][z], q);
-                } else if constexpr (SW::lShr) {
-                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
                 } else {
-                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkapz[z] * Tz), ft);
+                    ft = fma(ri, fma(K.kapz[z], lapT, K.dkz[z] * dTz), ft);  // dkz = dkapz cz1
                 }
             }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
