@@ -324,6 +324,13 @@ def run_ours(args, dist: Dist) -> None:
     L.mhd_host_free(hp)
     sim.close()
 
+    # the batching (config 2) and precision (config 3) forms, measured in the
+    # same run at their configured sizes and step counts
+    forms = {}
+    if dist.world == 1 and not args.no_forms:
+        forms["batch"] = measure_batch(args.batch_steps, args.serial_steps)
+        forms["precision"] = measure_precision(args.precision_steps)
+
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(case)
@@ -365,6 +372,7 @@ def run_ours(args, dist: Dist) -> None:
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    line.update(forms)
     print(json.dumps(line), flush=True)
 
 
@@ -382,11 +390,20 @@ TRAFFIC_OVER_ALGORITHMIC = {(True, True, True): 2.274 / 2.282}
 # precision form: FP32 storage vs the FP64 path on the 256x256x128 case
 # ---------------------------------------------------------------------------
 def run_precision(args, dist: Dist) -> None:
-    from mhd_gb300.sim import Simulation
     L = abi.load()
     abi.check(L.mhd_set_device(dist.local))
+    out = measure_precision(args.precision_steps)
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def measure_precision(nsteps: int) -> dict:
+    """Config 3: 256x256x128 lMag, noise 1e-2, `nsteps` fixed-dt steps with
+    FP64 storage and with FP32 storage (FP64 RK register, EOS and
+    reductions); per-field errors of the FP32 state against the FP64 one,
+    mass / energy drift and max |div B| before and after."""
+    from mhd_gb300.sim import Simulation
     case = config3()
-    nsteps = args.precision_steps
     st = initial_state(case)
     res = {}
     for prec in ("fp64", "fp32"):
@@ -442,20 +459,35 @@ def run_precision(args, dist: Dist) -> None:
                                       "ms_per_step": r["ms_cfl"] / 100,
                                       "cost_vs_fixed_dt": (r["ms_cfl"] / 100) / (r["ms"] / nsteps) - 1.0}}
     out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["fp32"]["vs_plain_fp64"] = out["speedup_fp32_over_fp64"]
+    out["fp64"]["vs_plain_fp64"] = 1.0
     out["errors_fp32_vs_fp64"] = errs
-    if dist.rank == 0:
-        print(json.dumps(out), flush=True)
+    out["max_l2_rel"] = max(e["l2_rel"] for e in errs.values())
+    out["value"] = out["fp32"]["value"]
+    out["ms_per_step"] = out["fp32"]["ms_per_step"]
+    out["vs_plain_fp64"] = out["speedup_fp32_over_fp64"]
+    return out
 
 
 # ---------------------------------------------------------------------------
 # batching form: 64 uneven instances, persistent launch per substage, graphs
 # ---------------------------------------------------------------------------
 def run_batch(args, dist: Dist) -> None:
-    from mhd_gb300.sim import Batch, Simulation
     L = abi.load()
     abi.check(L.mhd_set_device(dist.local))
+    out = measure_batch(args.batch_steps, args.serial_steps)
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def measure_batch(nsteps: int, serial_steps: int) -> dict:
+    """Config 2: 64 instances with the configuration's draw of sizes, seeds,
+    1/Re and Bz0, `nsteps` batched steps (one persistent launch per substage,
+    graph-captured, autotuned tile) with FP64 and with FP32 storage, against
+    the same instances stepped one after another on the plain FP64 path (a
+    bounded sample of `serial_steps` steps, scaled to `nsteps`)."""
+    from mhd_gb300.sim import Batch, Simulation
     cases = config2_batch()
-    nsteps = args.batch_steps
     sims = []
     for c in cases:
         s = Simulation(c)
@@ -474,7 +506,7 @@ def run_batch(args, dist: Dist) -> None:
     secs = time.perf_counter() - t
     b.close()
     # the plain single-instance path, instance after instance (a bounded sample of steps)
-    serial_steps = max(1, min(nsteps, args.serial_steps))
+    serial_steps = max(1, min(nsteps, serial_steps))
     for s in sims:
         s.steps(2, s.case.dt)
         s.sync()
@@ -515,8 +547,9 @@ def run_batch(args, dist: Dist) -> None:
            "speedup_vs_plain_serial": serial_secs / secs,
            "config": {"workload": "64 FP64 MHD instances, nx=ny in {32,48,64,96,128}, nz in {32,64}, "
                                   "1/Re log-uniform [3e-3,3e-2], Bz0 log-uniform [1e-4,1e-2]"}}
-    if dist.rank == 0:
-        print(json.dumps(out), flush=True)
+    out["vs_plain_fp64"] = out["speedup_vs_plain_serial"]
+    out["fp32_storage_batched"]["vs_plain_fp64"] = out["fp32_storage_batched"]["vs_plain_fp64_serial"]
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -569,6 +602,8 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batch and precision keys of the default line")
     args = ap.parse_args()
     dist = Dist()
     try:

@@ -47,7 +47,7 @@ extern "C" {
 #define MHD_SW_LROT 0x1u
 #define MHD_SW_LMAG 0x2u
 #define MHD_SW_LPOT 0x4u /* no effect: the reference never reads lPot */
-#define MHD_SW_LREM 0x8u /* not supported: MHD_ERR_UNSUPPORTED */
+#define MHD_SW_LREM 0x8u /* FP64 storage only; MHD_ERR_UNSUPPORTED with lShr or FP32 storage */
 #define MHD_SW_LSHR 0x10u
 
 /* storage precision of the state */
@@ -176,10 +176,15 @@ int mhd_cfl_dt(mhd_ctx* ctx, double* dt, double* umach);
  * same right-hand sides as mhd_fluxes, bit for bit, on device buffers the
  * caller owns, and allocates nothing.  Its scratch is a fixed device array
  * of MHD_NOALLOC_MAX_CELLS x 5 doubles (15.7 MB) inside the library, held by
- * every GPU that loads it until the process exits; grids with more than
- * MHD_NOALLOC_MAX_CELLS cells (ghosts included) are rejected with
- * MHD_ERR_INVALID and a message on stderr.  The first call on a device looks
- * up the array's address (make it before any stream capture).  All calls
+ * every GPU on which the entry point has run, until the process exits; grids
+ * with more than MHD_NOALLOC_MAX_CELLS cells (ghosts included) are rejected
+ * with MHD_ERR_INVALID and a message on stderr.  CUDA loads the library's
+ * device code lazily, so the FIRST call on a device is the one that loads it,
+ * reserves the 15.7 MB and looks up the array's address: make that call
+ * (any valid grid) before reserving the rest of the device's memory and
+ * before any stream capture.  The address is cached per device for the life
+ * of the process; after a cudaDeviceReset the cache is stale, so do not use
+ * this entry point again in a process that reset its device.  All calls
  * share the array: calls that overlap on the GPU race and must be serialised
  * by the caller.  Inputs are not modified (RO is only read; the reference
  * inverts it in place).  With lShr, flux[MHD_FT - 8] is read and accumulated,

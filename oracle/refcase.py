@@ -34,7 +34,9 @@ REPO = HERE.parent
 sys.path.insert(0, str(REPO / "rast-3dmhd-cpp_gb300" / "python"))
 from mhd_gb300.case import Case, STATE_FIELDS, FLUX_FIELDS, ZFIELDS, coordinates, metrics  # noqa: E402
 
-REF_DIR = Path(os.environ.get("MHD_REFERENCE_DIR", "/root/reference"))
+# the reference checkout: MHD_REFERENCE_DIR, else a "reference" directory beside
+# this repository
+REF_DIR = Path(os.environ.get("MHD_REFERENCE_DIR", str(REPO.parent / "reference")))
 OUT_DIR = HERE / "_ref"
 MAGIC = 0x3344484D
 

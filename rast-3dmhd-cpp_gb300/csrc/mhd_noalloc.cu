@@ -10,10 +10,14 @@
 // cell) live in the file-scope device array below instead of in a context.
 //
 // The array is MHD_NOALLOC_MAX_CELLS * 5 doubles (15.7 MB) and is held by
-// every GPU that loads this library, until the process exits.  Its device
-// address is looked up with cudaGetSymbolAddress the first time the entry
-// point runs on a device, with that device current; that first call should
-// therefore come before any stream capture.  The scratch keeps the last
+// every GPU on which this entry point has run, until the process exits.  CUDA
+// loads device code lazily, so the first call on a device loads this
+// module, reserves the array and looks up its device address with
+// cudaGetSymbolAddress (with that device current); callers make that first
+// call before their pool takes the rest of the device's memory and before any
+// stream capture.  The address is cached per device; it does not survive a
+// cudaDeviceReset, after which this entry point must not be used in the
+// same process.  The scratch keeps the last
 // call's contents: nothing in it has to start at zero, because each call
 // writes every scratch cell it later reads.  All calls share this one array,
 // so calls whose work overlaps on the GPU (different streams, or different

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference 3dmhd code itself.
 
-Run in a checkout that has the reference sources (default /root/reference,
-override with MHD_REFERENCE_DIR):
+Run where the reference sources are at hand (MHD_REFERENCE_DIR, else a
+"reference" directory beside this repository):
 
     python tests/golden/make_golden.py
 

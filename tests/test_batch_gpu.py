@@ -140,3 +140,46 @@ def test_fp32_batch_equals_instances_alone():
         for k in STATE_FIELDS:
             assert np.array_equal(got[i][k], ref[k]), (i, k)
             assert rel_err(got[i][k], pl[k]) <= 1e-6, (i, k)
+
+
+def config2_subset():
+    """Instances of the 64-instance ragged batch (nx = ny from
+    {32,48,64,96,128}, nz from {32,64}, per-instance seed, 1/Re and Bz0), one
+    of each distinct shape, so the tallest and widest ones (128x128x64) are in."""
+    from mhd_gb300.case import config2_batch
+    seen, out = set(), []
+    for c in config2_batch():
+        key = (c.nPx, c.nPz)
+        if key not in seen:
+            seen.add(key)
+            out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("tile", [0, 2])
+def test_batch_config2_shapes_against_the_oracle(tile):
+    """One batched step of config 2's real instance shapes, every instance
+    compared with the oracle directly: 1e-12 of each field's max-norm."""
+    from gpu_util import oracle_for
+    cases = config2_subset()
+    assert any(c.nPz == 64 for c in cases) and any(c.nPx == 128 for c in cases)
+    states = [initial_state(c) for c in cases]
+    sims = []
+    for c, st in zip(cases, states):
+        s = Simulation(c, path="fused")
+        s.upload_state(st)
+        s.communicate()
+        sims.append(s)
+    b = Batch(sims)
+    b.set_tile(tile)
+    b.steps(1)
+    b.sync()
+    got = [s.download_state() for s in sims]
+    b.close()
+    for s in sims:
+        s.close()
+    for c, st, g in zip(cases, states, got):
+        o = oracle_for(c, st, nthreads=16)
+        o.steps(1)
+        for k in STATE_FIELDS:
+            assert rel_err(g[k], o.arr[k]) <= 1e-12, (c.nPx, c.nPz, k, rel_err(g[k], o.arr[k]))

@@ -90,6 +90,44 @@ def test_noalloc_matches_mhd_fluxes_on_two_calls(name):
             assert np.array_equal(a, b), (call, k, float(np.abs(a - b).max()))
 
 
+def test_noalloc_call_takes_no_device_memory():
+    """After a first call on the device (which loads the module and with it
+    the scratch array), a further call leaves the device's free memory and
+    torch's allocation count unchanged."""
+    torch = pytest.importorskip("torch")
+    case = small_cases()["mhd_rot_shr"].replace(nPx=20, nPy=12, nPz=10, seed=21)
+    st = initial_state(case)
+    ft0 = np.zeros(case.shape)
+    _noalloc_fluxes(torch, case, st, ft0)  # the first call on this device
+    L = abi.load()
+    dev = torch.device("cuda:0")
+    a = abi.MhdFluxesNoallocArgs()
+    a.nPx, a.nPy, a.nPz = case.nPx, case.nPy, case.nPz
+    a.switches = abi.SW_LROT | abi.SW_LMAG | abi.SW_LSHR
+    a.izCon, a.iTCon, a.iBCon = case.izCon, case.iTCon, case.iBCon
+    for k in ("RE", "PR", "THETA", "GRAV", "RY", "ANG", "RM", "BETA", "TP", "GAMMA", "SFF"):
+        setattr(a, k, float(getattr(case, k)))
+    a.TB = case.tb
+    keep = [torch.from_numpy(np.ascontiguousarray(m, dtype=np.float64)).to(dev) for m in metrics(case).arrays()]
+    for n, t in zip(METRIC_NAMES, keep):
+        setattr(a, n, t.data_ptr())
+    for f, k in enumerate(STATE_FIELDS):
+        t = torch.from_numpy(st[k]).to(dev)
+        keep.append(t)
+        a.state[f] = t.data_ptr()
+    for f in range(8):
+        t = torch.zeros(case.shape, dtype=torch.float64, device=dev)
+        keep.append(t)
+        a.flux[f] = t.data_ptr()
+    torch.cuda.synchronize()
+    free0, used0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for _ in range(2):
+        assert L.mhd_fluxes_noalloc(C.byref(a), None) == abi.MHD_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == used0
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch():
     L = abi.load()
     a = abi.MhdFluxesNoallocArgs()
