@@ -56,6 +56,50 @@ __device__ __forceinline__ RingPtrs ring_slot(unsigned char* ring, int slot) {
     return {reinterpret_cast<float*>(b + (size_t)kPlane * sizeof(double)), reinterpret_cast<double*>(b)};
 }
 
+// Raw FP32 fields of one plane (8 with lMag, else 5), staged in shared
+// memory by asynchronous copies while the plane two ahead is computed.
+template <class SW>
+constexpr int nraw() {
+    return SW::lMag ? 8 : 5;
+}
+
+template <class SW>
+constexpr size_t smem_bytes() {
+    return 3 * plane_bytes<SW>() + (size_t)nraw<SW>() * kPlane * sizeof(float);
+}
+
+template <class SW>
+__device__ __forceinline__ float* raw_stage(unsigned char* ring) {
+    return reinterpret_cast<float*>(ring + 3 * plane_bytes<SW>());
+}
+
+// The derived quantities of one plane point from its raw fields (get(f) is
+// field f of the point): 1/rho and the velocities in FP32, p = rho T in FP64.
+template <class SW, class Get>
+__device__ __forceinline__ void put_point(RingPtrs r, int k, double r0, double t0, Get get) {
+    const float ru = get(S_RU), rv = get(S_RV), rw = get(S_RW);
+    const float dt = get(S_TT), dro = get(S_RO);
+    const double ro = r0 + widen_f32(dro), tt = t0 + widen_f32(dt);
+    const float ri = 1.0f / narrow_f64(ro);
+    r.p[k] = ro * tt;
+    r.f[F_RU * kPlane + k] = ru;
+    r.f[F_RV * kPlane + k] = rv;
+    r.f[F_RW * kPlane + k] = rw;
+    r.f[F_DT * kPlane + k] = dt;
+    r.f[F_DRO * kPlane + k] = dro;
+    r.f[F_RI * kPlane + k] = ri;
+    r.f[F_U * kPlane + k] = ru * ri;
+    r.f[F_V * kPlane + k] = rv * ri;
+    r.f[F_W * kPlane + k] = rw * ri;
+    if constexpr (SW::lMag) {
+        r.f[F_BX * kPlane + k] = get(S_BX);
+        r.f[F_BY * kPlane + k] = get(S_BY);
+        r.f[F_BZ * kPlane + k] = get(S_BZ);
+    }
+}
+
+// Plane z into ring slot `slot`, read directly from global memory (the first
+// three planes of a z range).
 template <class SW>
 __device__ __forceinline__ void load_plane32(const Fused32Args& a, unsigned char* ring, int slot, int z, int x0,
                                              int y0) {
@@ -67,25 +111,45 @@ __device__ __forceinline__ void load_plane32(const Fused32Args& a, unsigned char
         const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
         if (gx >= g.nx || gy >= g.ny) continue;
         const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
-        const float ru = a.U.p[S_RU][i], rv = a.U.p[S_RV][i], rw = a.U.p[S_RW][i];
-        const float dt = a.U.p[S_TT][i], dro = a.U.p[S_RO][i];
-        const double ro = r0 + widen_f32(dro), tt = t0 + widen_f32(dt);
-        const float ri = 1.0f / narrow_f64(ro);
-        r.p[k] = ro * tt;
-        r.f[F_RU * kPlane + k] = ru;
-        r.f[F_RV * kPlane + k] = rv;
-        r.f[F_RW * kPlane + k] = rw;
-        r.f[F_DT * kPlane + k] = dt;
-        r.f[F_DRO * kPlane + k] = dro;
-        r.f[F_RI * kPlane + k] = ri;
-        r.f[F_U * kPlane + k] = ru * ri;
-        r.f[F_V * kPlane + k] = rv * ri;
-        r.f[F_W * kPlane + k] = rw * ri;
-        if constexpr (SW::lMag) {
-            r.f[F_BX * kPlane + k] = a.U.p[S_BX][i];
-            r.f[F_BY * kPlane + k] = a.U.p[S_BY][i];
-            r.f[F_BZ * kPlane + k] = a.U.p[S_BZ][i];
+        put_point<SW>(r, k, r0, t0, [&](int f) { return a.U.p[f][i]; });
+    }
+}
+
+// Start the asynchronous copies (cp.async, 4 bytes each: the rows of an
+// unpadded FP32 field are not 16-byte aligned) of plane z's raw fields into
+// the staging area.  Every thread copies the points it later derives itself,
+// so its own cp.async.wait_all is the only wait the derivation needs.
+template <class SW>
+__device__ __forceinline__ void stage_plane32(const Fused32Args& a, unsigned char* ring, int z, int x0, int y0) {
+    float* raw = raw_stage<SW>(ring);
+    const Grid& g = a.g;
+    for (int k = threadIdx.x; k < kPlane; k += kThreads) {
+        const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
+        if (gx >= g.nx || gy >= g.ny) continue;
+        const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
+#pragma unroll
+        for (int f = 0; f < nraw<SW>(); f++) {
+            const unsigned dst = (unsigned)__cvta_generic_to_shared(raw + f * kPlane + k);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(a.U.p[f] + i) : "memory");
         }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// Wait for this thread's staged copies of plane z and derive its points into
+// ring slot `slot`.
+template <class SW>
+__device__ __forceinline__ void derive_plane32(const Fused32Args& a, unsigned char* ring, int slot, int z, int x0,
+                                               int y0) {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    const float* raw = raw_stage<SW>(ring);
+    RingPtrs r = ring_slot<SW>(ring, slot);
+    const Grid& g = a.g;
+    const double r0 = a.bgR[z], t0 = a.bgT[z];
+    for (int k = threadIdx.x; k < kPlane; k += kThreads) {
+        const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
+        if (gx >= g.nx || gy >= g.ny) continue;
+        put_point<SW>(r, k, r0, t0, [&](int f) { return raw[f * kPlane + k]; });
     }
 }
 
@@ -146,16 +210,8 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
     const int pc = (ty + 1) * kPX + (tx + 1);
     for (int z = zb; z < ze; z++) {
         __syncthreads();
-        if (z + 2 <= ze) {  // the points of plane z+2 this thread loads after the compute below
-            for (int k = threadIdx.x; k < kPlane; k += kThreads) {
-                const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
-                if (gx >= g.nx || gy >= g.ny) continue;
-                const long long ip = (long long)(z + 2) * g.sz + (long long)gy * g.sy + gx;
-                constexpr int nfp = SW::lMag ? 8 : 5;
-#pragma unroll
-                for (int f = 0; f < nfp; f++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.U.p[f] + ip));
-            }
-        }
+        // plane z+2's raw fields land in the staging area while plane z computes
+        if (z + 2 <= ze) stage_plane32<SW>(a, ring, z + 2, x0, y0);
         if (active) {
             const RingPtrs Rm = ring_slot<SW>(ring, (z - 1) % 3);
             const RingPtrs R0 = ring_slot<SW>(ring, z % 3);
@@ -359,7 +415,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             }
         }
         __syncthreads();
-        if (z + 2 <= ze) load_plane32<SW>(a, ring, (z + 2) % 3, z + 2, x0, y0);
+        if (z + 2 <= ze) derive_plane32<SW>(a, ring, (z + 2) % 3, z + 2, x0, y0);
     }
 }
 
@@ -524,7 +580,7 @@ int chunks32(long long tiles, int slots, int nPz) {
 
 template <class SW, bool EXTRA>
 void launch32_t(const Fused32Args& a, cudaStream_t st, int* rc) {
-    const size_t smem = 3 * plane_bytes<SW>();
+    const size_t smem = smem_bytes<SW>();
     static int slots = 0;
     if (!slots) {
         cudaFuncSetAttribute(k_substage32<SW, EXTRA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -556,13 +612,13 @@ void launch_bcon32(const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const 
 template <class SW>
 void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, int grid, cudaStream_t st,
                     int* rc) {
-    k_substage32_batch<SW><<<grid, kThreads, 3 * plane_bytes<SW>(), st>>>(args, items, nitems, counter);
+    k_substage32_batch<SW><<<grid, kThreads, smem_bytes<SW>(), st>>>(args, items, nitems, counter);
     *rc = (int)cudaGetLastError();
 }
 
 template <class SW>
 void batch32_occupancy(int* blocks, int* rc) {
-    const size_t smem = 3 * plane_bytes<SW>();
+    const size_t smem = smem_bytes<SW>();
     cudaFuncSetAttribute(k_substage32_batch<SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     *rc = (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_substage32_batch<SW>, kThreads, smem);
 }
