@@ -171,24 +171,46 @@ def cpu_sample_case(case):
     return case.replace(nPz=16, name=case.name + "_slab16")
 
 
+ORACLE_FLAGS = "gcc -O2 -std=gnu11 -ffp-contract=off -fno-fast-math -fopenmp"
+
+
+def _time_oracle_steps(o, n: int, dt: float | None) -> float:
+    t = time.perf_counter()
+    o.steps(n, dt)
+    return time.perf_counter() - t
+
+
 def cpu_baseline(case, target_s: float = 12.0, threads: int | None = None) -> dict:
+    """The reference's algorithm (the oracle) on the host cores, in the two
+    run modes of the reference: the configuration's fixed dt, and the CFL dt
+    of step() (3dmhdsub.h:36-106) computed every step, reduced over all
+    threads (plane-parallel, the same DT as the serial order)."""
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
     threads = threads or os.cpu_count() or 1
     sc = cpu_sample_case(case)
     st = initial_state(sc)
     o = oracle.OracleSim(sc, st, nthreads=threads)
+    o.p.cfl_parallel = 1
     o.communicate()
-    t = time.perf_counter()
-    o.steps(1)
-    t1 = time.perf_counter() - t
+    t1 = _time_oracle_steps(o, 1, None)
     n = max(1, min(50, int(target_s / max(t1, 1e-3))))
-    t = time.perf_counter()
-    o.steps(n)
-    secs = time.perf_counter() - t
+    secs = _time_oracle_steps(o, n, None)
+    # the reference's default run mode: a CFL dt for every step
+    o2 = oracle.OracleSim(sc, st, nthreads=threads)
+    o2.p.cfl_parallel = 1
+    o2.communicate()
+    _time_oracle_steps(o2, 1, -1.0)
+    ncfl = max(1, n // 2)
+    secs_cfl = _time_oracle_steps(o2, ncfl, -1.0)
     return {"value": sc.cells * n / secs, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{sc.nPx}x{sc.nPy}x{sc.nPz} slab of the workload (same physics), {n} RK3 steps after 1 warm-up, "
-                      f"oracle/mhd_oracle.c with OpenMP over {threads} threads, {secs:.1f} s"}
+            "flags": ORACLE_FLAGS,
+            "sample": f"{sc.nPx}x{sc.nPy}x{sc.nPz} slab of the workload (same physics), {n} fixed-dt RK3 steps after "
+                      f"1 warm-up, oracle/mhd_oracle.c with OpenMP over {threads} threads, {secs:.1f} s",
+            "cfl_dt": {"value": sc.cells * ncfl / secs_cfl, "unit": METRIC, "steps": ncfl,
+                       "ms_per_step": 1e3 * secs_cfl / ncfl, "cost_vs_fixed_dt": (secs_cfl / ncfl) / (secs / n) - 1.0,
+                       "sample": f"the same slab, {ncfl} RK3 steps each with the CFL dt of step() "
+                                 f"(3dmhdsub.h:36-106), the reduction over {threads} threads"}}
 
 
 def run_reference(args, dist: Dist) -> None:
@@ -201,19 +223,29 @@ def run_reference(args, dist: Dist) -> None:
     sc = cpu_sample_case(case)
     st = initial_state(sc)
     o = oracle.OracleSim(sc, st, nthreads=threads)
+    o.p.cfl_parallel = 1
     o.communicate()
     o.steps(max(1, args.warmup))
-    t = time.perf_counter()
-    o.steps(args.steps)
-    secs = time.perf_counter() - t
+    secs = _time_oracle_steps(o, args.steps, None)
     value = sc.cells * args.steps / secs
+    # the reference's default run mode (CFL dt every step) on the same slab
+    o2 = oracle.OracleSim(sc, st, nthreads=threads)
+    o2.p.cfl_parallel = 1
+    o2.communicate()
+    o2.steps(1, -1.0)
+    secs_cfl = _time_oracle_steps(o2, args.steps, -1.0)
     sample = (f"each step: one RK3 step of a {sc.nPx}x{sc.nPy}x{sc.nPz} slab of the {case.name} workload "
               f"(same physics), oracle/mhd_oracle.c (bit-exact restatement of the reference) on {threads} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(case, args),
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample,
+                             "flags": ORACLE_FLAGS,
+                             "cfl_dt": {"value": sc.cells * args.steps / secs_cfl, "unit": METRIC,
+                                        "ms_per_step": 1e3 * secs_cfl / args.steps,
+                                        "sample": "the same slab and steps, each with the CFL dt of step() "
+                                                  "(3dmhdsub.h:36-106)"}},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -330,6 +362,9 @@ def run_ours(args, dist: Dist) -> None:
     if dist.world == 1 and not args.no_forms:
         forms["batch"] = measure_batch(args.batch_steps, args.serial_steps)
         forms["precision"] = measure_precision(args.precision_steps)
+        # the batch's FP64 rate per cell against one instance of the same physics
+        # (lMag, 256x256x128 FP64 in the precision form)
+        forms["batch"]["vs_single_instance_same_physics"] = forms["batch"]["value"] / forms["precision"]["fp64"]["value"]
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -497,6 +532,7 @@ def measure_batch(nsteps: int, serial_steps: int) -> dict:
     cells = sum(c.cells for c in cases)
     b = Batch(sims)
     chosen, tile_ms = b.autotune()
+    zrange = b.zrange()
     b.steps(3)
     b.sync()
     sims[0].timer_start()
@@ -525,7 +561,8 @@ def measure_batch(nsteps: int, serial_steps: int) -> dict:
         s.communicate()
         sims32.append(s)
     b32 = Batch(sims32)
-    b32.set_tile(0)
+    _, tile32_ms = b32.autotune()
+    zrange32 = b32.zrange()
     b32.steps(3)
     b32.sync()
     t = time.perf_counter()
@@ -541,7 +578,9 @@ def measure_batch(nsteps: int, serial_steps: int) -> dict:
                                     "vs_fp64_batched": secs / secs32},
            "cells_per_step": cells, "dtype": "f64",
            "value": cells * nsteps / secs, "ms_per_step": 1e3 * secs / nsteps,
-           "autotune": {"chosen": ["32x4", "32x8", "16x8"][chosen], "ms_per_step_by_tile": tile_ms},
+           "autotune": {"chosen": ["32x4", "32x8", "16x8"][chosen], "zrange": zrange,
+                        "ms_per_step_by_tile": tile_ms, "fp32_zrange": zrange32,
+                        "fp32_ms_per_step": tile32_ms[0]},
            "plain_serial": {"value": cells * nsteps / serial_secs, "ms_per_step": 1e3 * serial_secs / nsteps,
                             "sample_steps": serial_steps},
            "speedup_vs_plain_serial": serial_secs / secs,
@@ -556,32 +595,62 @@ def measure_batch(nsteps: int, serial_steps: int) -> dict:
 # serving form: Poisson request stream, continuous batching under an HBM budget
 # ---------------------------------------------------------------------------
 def run_serve(args, dist: Dist) -> None:
+    """Config 4: the Poisson request stream served with continuous batching
+    under a 150 GB HBM budget.  Baseline: the same requests one after another
+    on the plain FP64 path -- all of them for a short stream, else a seeded
+    random sample of --serve-serial-sample requests, timed per cell-step and
+    scaled to the stream's cell-steps."""
     from mhd_gb300.serve import Server, poisson_requests, run_serial
     L = abi.load()
     abi.check(L.mhd_set_device(dist.local))
     n = args.serve_requests
     smin, smax = max(1, 50 // args.serve_step_scale), max(2, 2000 // args.serve_step_scale)
-    reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
-    srv = Server(150 << 30, quantum=25, policy="srpt")
+
+    def stream():
+        return poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
+
+    log = open(args.serve_progress, "a") if args.serve_progress else None
+
+    def progress(d):
+        if log:
+            log.write(json.dumps(d) + "\n")
+            log.flush()
+    reqs = stream()
+    srv = Server(150 << 30, quantum=25, policy="srpt", progress=progress)
     st = srv.run(reqs, realtime=True)
-    # the same stream admitted first come, first served (everything resident shares the GPU)
-    fifo_reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
-    fifo = Server(150 << 30, quantum=25, policy="fifo", tile=st["tile"]).run(fifo_reqs, realtime=True)
+    progress({"done": "srpt", **{k: st[k] for k in ("value", "wall_s", "tts_p50_s", "tts_p99_s")}})
+    fifo = None
+    if args.serve_fifo:
+        fifo = Server(150 << 30, quantum=25, policy="fifo", tile=st["tile"]).run(stream(), realtime=True)
     # baseline: the same requests one after another on the plain FP64 path
-    serial_reqs = poisson_requests(n, rate=20.0, seed=4, steps=(smin, smax), fp32_fraction=0.5)
-    base = run_serial(serial_reqs)
+    all_reqs = stream()
+    total_cs = sum(r.case.cells * r.steps for r in all_reqs)
+    if args.serve_serial_sample and args.serve_serial_sample < n:
+        rng = np.random.default_rng(7)
+        pick = sorted(rng.choice(n, size=args.serve_serial_sample, replace=False))
+        sample = [all_reqs[i] for i in pick]
+        base = run_serial(sample)
+        base = {"value": base["value"], "sample_requests": len(sample), "sample_wall_s": base["wall_s"],
+                "sample_cell_steps": base["cell_steps"], "wall_s_scaled": total_cs / base["value"],
+                "note": "seeded random sample of the stream, timed per cell-step, scaled to the whole stream"}
+    else:
+        base = run_serial(all_reqs)
+    steps_ms = [r.steps for r in reqs]
     out = {"form": "serve", "metric": METRIC, "unit": METRIC, "requests": n, "rate_per_s": 20.0,
-           "steps_range": [smin, smax], "hbm_budget_gb": 150,
+           "steps_range": [smin, smax], "hbm_budget_gb": 150, "cell_steps": total_cs,
            "value": st["value"], "wall_s": st["wall_s"], "tts_p50_s": st["tts_p50_s"],
            "tts_p99_s": st["tts_p99_s"], "max_resident": st["max_resident"], "tile": st["tile"],
-           "batch_rebuilds": st["batch_rebuilds"], "policy": st["policy"],
-           "target_cells": srv.target_cells,
-           "fifo": {k: fifo[k] for k in ("value", "wall_s", "tts_p50_s", "tts_p99_s", "max_resident",
-                                          "batch_rebuilds")},
+           "zrange": st["zrange"], "batch_rebuilds": st["batch_rebuilds"], "policy": st["policy"],
+           "target_cells": srv.target_cells, "mean_steps": float(np.mean(steps_ms)),
            "serial_plain_fp64": base, "throughput_vs_serial": st["value"] / base["value"],
            "config": {"workload": f"Poisson stream of {n} simulations at 20/s, grids log-uniform 32^3..256^2x128, "
-                                  f"steps uniform [{smin},{smax}] (the configured [50,2000] / "
-                                  f"{args.serve_step_scale}), half FP32 storage, random seeds and 1/Re"}}
+                                  f"steps uniform [{smin},{smax}]"
+                                  + (f" (the configured [50,2000] / {args.serve_step_scale})"
+                                     if args.serve_step_scale != 1 else "")
+                                  + ", half FP32 storage, random seeds and 1/Re"}}
+    if fifo:
+        out["fifo"] = {k: fifo[k] for k in ("value", "wall_s", "tts_p50_s", "tts_p99_s", "max_resident",
+                                            "batch_rebuilds")}
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -599,6 +668,10 @@ def main():
     ap.add_argument("--serial-steps", type=int, default=20)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-step-scale", type=int, default=10)
+    ap.add_argument("--serve-serial-sample", type=int, default=0,
+                    help="time the serial baseline on this many sampled requests (0 = all)")
+    ap.add_argument("--serve-fifo", action="store_true", help="also serve the stream first come, first served")
+    ap.add_argument("--serve-progress", default=None, help="append running totals (JSON lines) to this file")
     ap.add_argument("--precision-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

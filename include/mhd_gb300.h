@@ -317,13 +317,27 @@ typedef struct mhd_batch mhd_batch;
 int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* stream, mhd_batch** out);
 int mhd_batch_destroy(mhd_batch* b);
 /* tile shape: -1 = autotune on the next step, 0 = 32x4, 1 = 32x8, 2 = 16x8
- * (FP32-storage batches always use 32x8) */
+ * (FP32-storage batches: 32x8, accepted as 0) */
 int mhd_batch_set_tile(mhd_batch* b, int tile);
 int mhd_batch_tile(const mhd_batch* b, int* tile);
-/* Time every tile shape (ms_per_step, may be NULL, gets one entry per shape)
- * and keep the fastest. */
+/* longest z range of a work item, in planes (default 64): an instance with
+ * more interior planes is split into about equal ranges of at most zmax */
+int mhd_batch_set_zrange(mhd_batch* b, int zmax);
+int mhd_batch_zrange(const mhd_batch* b, int* zmax);
+/* Time every candidate (tile shape x longest z range 64 / 32 / 16) on a
+ * scratch copy of the batch and keep the fastest; ms_per_step (may be NULL,
+ * 3 entries) gets the best time per step of each tile shape (0 where a shape
+ * is not a candidate), chosen the tile shape.  With ms_per_step NULL a
+ * result cached for the same batch signature is reused. */
 int mhd_batch_autotune(mhd_batch* b, int* chosen, double* ms_per_step);
+/* device bytes the autotuner's scratch copy takes while it runs */
+int mhd_batch_autotune_bytes(const mhd_batch* b, unsigned long long* bytes);
 int mhd_batch_steps(mhd_batch* b, int nsteps);
+/* nsteps batched steps in which instance i takes only its first
+ * min(nsteps, max_steps[i]) (host array of n counts): an instance that reaches
+ * its count drops out of the work list for the rest of the call, so a
+ * server's quantum need not shrink to the shortest remaining request. */
+int mhd_batch_steps_limited(mhd_batch* b, int nsteps, const int* max_steps);
 int mhd_batch_sync(mhd_batch* b);
 
 /* ---- device selection and timing ---------------------------------------- */

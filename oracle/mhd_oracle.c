@@ -546,13 +546,16 @@ static inline double dmin(double a, double b) { return (b < a) ? b : a; }
 static inline double dmax(double a, double b) { return (a < b) ? b : a; }
 
 /* CFL section of step(), 3dmhdsub.h:36-106 (ISW == 1) */
-double orc_cfl_dt(const orc_params* p, orc_fields* f, double* umach) {
+/* The CFL candidates of planes z in [z0, z1), folded in the reference's cell
+ * order into r[0] = UMACH^2 max, r[1..4] = the four minima (3dmhdsub.h:36-106). */
+static void cfl_planes(const orc_params* p, orc_fields* f, int z0, int z1, double r[5]) {
     DECL_DIMS;
+    (void)nz;
     const double *RU = f->a[ORC_RU], *RV = f->a[ORC_RV], *RW = f->a[ORC_RW], *TT = f->a[ORC_TT], *RO = f->a[ORC_RO];
     const double *BX = f->a[ORC_BX], *BY = f->a[ORC_BY], *BZ = f->a[ORC_BZ];
     const double OGAMMA = 1.0f / p->GAMMA;
-    double um = 0.0f, w0 = 1e99, w1 = 1e99, w2 = 1e99, w3 = 1e99;
-    for (int z = 1; z < nz - 1; z++)
+    double um = r[0], w0 = r[1], w1 = r[2], w2 = r[3], w3 = r[4];
+    for (int z = z0; z < z1; z++)
         for (int y = 1; y < ny - 1; y++)
             for (int x = 1; x < nx - 1; x++) {
                 const size_t i = ((size_t)z * ny + y) * nx + x;
@@ -572,9 +575,35 @@ double orc_cfl_dt(const orc_params* p, orc_fields* f, double* umach) {
                 w2 = dmin(w2, 0.375f * DD * DD * p->RE * RO[i]);
                 if (p->lMag) w3 = dmin(w3, 0.5f * DD * DD * p->RM);
             }
-    if (umach) *umach = sqrt(um);
-    if (p->lMag) return p->SFF * dmin(dmin(w0, w1), dmin(w2, w3));
-    return p->SFF * dmin(dmin(w0, w1), w2);
+    r[0] = um; r[1] = w0; r[2] = w1; r[3] = w2; r[4] = w3;
+}
+
+double orc_cfl_dt(const orc_params* p, orc_fields* f, double* umach) {
+    const int nz = p->nz;
+    double r[5] = {0.0f, 1e99, 1e99, 1e99, 1e99};
+    if (p->cfl_parallel) {
+        /* every plane on its own thread from the neutral start, then folded in
+         * plane order: min/max of finite values do not depend on the grouping */
+        double* part = (double*)malloc(sizeof(double) * 5 * (size_t)nz);
+        set_threads(p);
+        ORC_PRAGMA(omp parallel for schedule(static))
+        for (int z = 1; z < nz - 1; z++) {
+            double* q = part + 5 * (size_t)z;
+            q[0] = 0.0f; q[1] = q[2] = q[3] = q[4] = 1e99;
+            cfl_planes(p, f, z, z + 1, q);
+        }
+        for (int z = 1; z < nz - 1; z++) {
+            const double* q = part + 5 * (size_t)z;
+            r[0] = dmax(r[0], q[0]);
+            for (int k = 1; k < 5; k++) r[k] = dmin(r[k], q[k]);
+        }
+        free(part);
+    } else {
+        cfl_planes(p, f, 1, nz - 1, r);
+    }
+    if (umach) *umach = sqrt(r[0]);
+    if (p->lMag) return p->SFF * dmin(dmin(r[1], r[2]), dmin(r[3], r[4]));
+    return p->SFF * dmin(dmin(r[1], r[2]), r[3]);
 }
 
 int orc_steps(const orc_params* p0, orc_fields* f, int n, double dt, double* timt, double* dt_out) {

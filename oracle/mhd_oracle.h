@@ -24,7 +24,9 @@ typedef struct orc_params {
     int lMag, lRot, lShr;
     int izCon, iTCon, iBCon;
     int nthreads;        /* OpenMP threads, <=0 leaves the runtime default */
-    int pad_;
+    int cfl_parallel;    /* 1: orc_cfl_dt reduces planes on all threads (the same
+                            result for finite states; with NaN/Inf only the default
+                            serial order is the reference's) -- timing runs only */
     /* scalars as set() and main() leave them (3dmhd.cpp:144-145,354-369,401-459) */
     double C13, C23, C43, GAM1, GAM2, GAM3, ZETA1, ZETA2;
     double hx, h2x, hy, h2y, hz, h2z;

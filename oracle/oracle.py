@@ -43,7 +43,7 @@ def build(force: bool = False) -> Path:
 
 class OrcParams(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nx", "ny", "nz", "nPz", "lMag", "lRot", "lShr", "izCon", "iTCon",
-                                        "iBCon", "nthreads", "pad_")] + \
+                                        "iBCon", "nthreads", "cfl_parallel")] + \
                [(n, C.c_double) for n in ("C13", "C23", "C43", "GAM1", "GAM2", "GAM3", "ZETA1", "ZETA2",
                                            "hx", "h2x", "hy", "h2y", "hz", "h2z",
                                            "RE", "PR", "REPR", "ORE", "CV", "OCV", "GAMMA", "GRAV", "THETA",

@@ -163,14 +163,18 @@ int fused_substage_xp(unsigned sw, const FusedArgs& a, cudaStream_t st);
 constexpr int kBatchTiles = 3;
 void batch_tile_dims(int tile, int* tx, int* ty);
 // _uxy: uniform x/y grids (d2xxdx2 = d2yydy2 = 0); _gen: any grid.
-// Item w = first z plane | (end plane << 16).
+// Item w = first z plane | (end plane << 16).  left[i] (device, one per
+// instance): the steps instance i still takes; its items are skipped at 0.
 int fused_batch_substage_uxy(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
-                             int grid, cudaStream_t st);
+                             const int* left, int grid, cudaStream_t st);
 int fused_batch_substage_gen(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
-                             int grid, cudaStream_t st);
+                             const int* left, int grid, cudaStream_t st);
 int fused_batch_occupancy_uxy(unsigned sw, int tile, int* blocks_per_sm);
 int fused_batch_occupancy_gen(unsigned sw, int tile, int* blocks_per_sm);
-int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, int nblocks, cudaStream_t st);
+int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, const int* left, int nblocks,
+                     cudaStream_t st);
+// end of a batched step: left[i] -= 1 where positive
+int batch_tick(int* left, int n, cudaStream_t st);
 int fused_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, cudaStream_t st);
 // BCON of one wall (0 = bottom plane 1, 1 = top plane nz-2) or both (wall = -1)
 int fused_bcon_wall(unsigned sw, const Grid& g, const Consts& c, Fields8 U, double timt, int wall, cudaStream_t st);
@@ -205,10 +209,11 @@ int communicate32(int nf, const Grid& g, Fields8f U, cudaStream_t st);
 // ragged batches of FP32-storage instances (tile 32x8; same item and counter
 // conventions as the FP64 batch)
 constexpr int kBatch32TX = 32, kBatch32TY = 8;
-int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter, int grid,
-                           cudaStream_t st);
+int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter,
+                           const int* left, int grid, cudaStream_t st);
 int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm);
-int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st);
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, const int* left, int nblocks,
+                       cudaStream_t st);
 // CFL reduction of an FP32-storage state (the FP64 row kernel on the widened
 // fields): out5 as parity_cfl, or the device time-step record as cfl_dt_on_device
 int cfl32_rows(bool mag, const Grid& g, const Consts& c, Fields8f U, const double* bgR, const double* bgT,

@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_substage32(Fused32Args a) {
 template <class SW>
 __global__ void __launch_bounds__(kThreads, 3) k_substage32_batch(const Fused32Args* __restrict__ args,
                                                                const int4* __restrict__ items, int nitems,
-                                                               int* counter) {
+                                                               int* counter, const int* __restrict__ left) {
     extern __shared__ __align__(16) unsigned char ring[];
     __shared__ int s_item;
     for (;;) {
@@ -444,6 +444,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_substage32_batch(const Fused32A
         __syncthreads();
         if (t >= nitems) break;
         const int4 it = items[t];
+        if (left[it.x] <= 0) continue;  // the instance has taken its steps (uniform over the CTA)
         substage32_tile<SW>(args[it.x], it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
         __syncthreads();
     }
@@ -523,8 +524,10 @@ __global__ void k_bcon_ghost32(Grid g, Consts c, Fields8f U, Fields8 Z, const do
 
 // BCON for a ragged batch: block b covers 128 wall cells of instance items[b].x from cell items[b].y
 template <class SW>
-__global__ void k_bcon_ghost32_batch(const Fused32Args* __restrict__ args, const int2* __restrict__ items) {
+__global__ void k_bcon_ghost32_batch(const Fused32Args* __restrict__ args, const int2* __restrict__ items,
+                                     const int* __restrict__ left) {
     const int2 it = items[blockIdx.x];
+    if (left[it.x] <= 0) return;
     const Fused32Args& a = args[it.x];
     const int nPx = a.g.nx - 2, nPy = a.g.ny - 2;
     const int t = it.y + threadIdx.x;
@@ -610,9 +613,9 @@ void launch_bcon32(const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const 
 }
 
 template <class SW>
-void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, int grid, cudaStream_t st,
-                    int* rc) {
-    k_substage32_batch<SW><<<grid, kThreads, smem_bytes<SW>(), st>>>(args, items, nitems, counter);
+void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, const int* left, int grid,
+                    cudaStream_t st, int* rc) {
+    k_substage32_batch<SW><<<grid, kThreads, smem_bytes<SW>(), st>>>(args, items, nitems, counter, left);
     *rc = (int)cudaGetLastError();
 }
 
@@ -624,16 +627,16 @@ void batch32_occupancy(int* blocks, int* rc) {
 }
 
 template <class SW>
-void batch32_bcon(const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st) {
-    k_bcon_ghost32_batch<SW><<<nblocks, 128, 0, st>>>(args, items);
+void batch32_bcon(const Fused32Args* args, const int2* items, const int* left, int nblocks, cudaStream_t st) {
+    k_bcon_ghost32_batch<SW><<<nblocks, 128, 0, st>>>(args, items, left);
 }
 
 }  // namespace
 
-int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter, int grid,
-                           cudaStream_t st) {
+int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter,
+                           const int* left, int grid, cudaStream_t st) {
     int rc = 0;
-    MHD_DISPATCH_SW(sw, batch32_launch, args, items, nitems, counter, grid, st, &rc);
+    MHD_DISPATCH_SW(sw, batch32_launch, args, items, nitems, counter, left, grid, st, &rc);
     return rc;
 }
 
@@ -643,8 +646,9 @@ int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm) {
     return rc;
 }
 
-int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, int nblocks, cudaStream_t st) {
-    MHD_DISPATCH_SW(sw, batch32_bcon, args, items, nblocks, st);
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, const int* left, int nblocks,
+                       cudaStream_t st) {
+    MHD_DISPATCH_SW(sw, batch32_bcon, args, items, left, nblocks, st);
     return (int)cudaGetLastError();
 }
 

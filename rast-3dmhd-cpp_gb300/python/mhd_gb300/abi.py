@@ -127,6 +127,10 @@ SIGNATURES = {
     "mhd_batch_tile": [C.c_void_p, C.POINTER(C.c_int)],
     "mhd_batch_autotune": [C.c_void_p, C.POINTER(C.c_int), _DP],
     "mhd_batch_steps": [C.c_void_p, C.c_int],
+    "mhd_batch_steps_limited": [C.c_void_p, C.c_int, C.POINTER(C.c_int)],
+    "mhd_batch_set_zrange": [C.c_void_p, C.c_int],
+    "mhd_batch_zrange": [C.c_void_p, C.POINTER(C.c_int)],
+    "mhd_batch_autotune_bytes": [C.c_void_p, C.POINTER(C.c_ulonglong)],
     "mhd_batch_sync": [C.c_void_p],
     "mhd_write_dat0": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_int],
     "mhd_read_dat0": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_int],

@@ -106,14 +106,22 @@ class Server:
 
     quantum: at most this many steps are queued per resident simulation
     between scheduling decisions (admissions and completions happen between
-    quanta).  tile: batch tile shape (None = the 16x8 tile until an FP64
-    batch holds at least a quarter of target_cells, then the autotuner's
-    choice on that batch, kept for the rest of the run: a tuning on the first,
-    often tiny, batch would fix a shape that suits a handful of small grids)."""
+    quanta); a simulation with fewer steps left takes only those and drops
+    out of the batch's work for the rest of the quantum, so one nearly
+    finished request does not shorten the quantum of all others.  tile: FP64
+    batch tile shape (None = the 16x8 tile until an FP64 batch holds at least
+    a quarter of target_cells, then the autotuner's choice of tile shape and
+    z range on that batch, kept for the rest of the run: a tuning on the
+    first, often tiny, batch would fix a shape that suits a handful of small
+    grids); FP32-storage batches tune their z range the same way.  The
+    autotuner's scratch copy of the batch counts against the HBM budget while
+    it runs: when it does not fit, the batch keeps the default and tuning is
+    tried again at the next rebuild.  progress: optional callable receiving a
+    dict of running totals every progress_s seconds."""
 
     def __init__(self, hbm_budget_bytes: int, quantum: int = 25, tile: int | None = None,
                  keep_results: bool = False, device_init: bool = True, policy: str = "srpt",
-                 target_cells: int = 64_000_000):
+                 target_cells: int = 64_000_000, progress=None, progress_s: float = 30.0):
         if policy not in ("fifo", "srpt"):
             raise ValueError(f"unknown admission policy {policy!r}")
         self.policy = policy
@@ -122,7 +130,12 @@ class Server:
         self.budget = int(hbm_budget_bytes)
         self.quantum = int(quantum)
         self.tile = tile
-        self.tuned = tile is not None
+        self.tuned = {"fp64": tile is not None, "fp32": False}
+        self.zrange = {"fp64": None, "fp32": None}
+        self.progress = progress
+        self.progress_s = float(progress_s)
+        self.completed = 0
+        self.tune_skipped = 0
         self.keep_results = keep_results
         self.device_init = device_init
         self.used = 0
@@ -160,6 +173,7 @@ class Server:
         self.used -= r.nbytes
         self.resident_cells -= r.req.case.cells
         r.req.t_done = now
+        self.completed += 1
         del self.resident[r.req.rid]
 
     def _groups(self):
@@ -179,27 +193,37 @@ class Server:
         for key, rids in groups.items():
             if key not in self.batches:
                 b = Batch([self.resident[r].sim for r in rids])
-                if key[0] == "fp64":
-                    if not self.tuned and sum(self.resident[r].sim.case.cells for r in rids) >= self.target_cells // 4:
-                        self.tile, _ = b.autotune(report=False)
-                        self.tuned = True
+                prec = key[0]
+                if not self.tuned[prec] and sum(self.resident[r].sim.case.cells for r in rids) >= self.target_cells // 4:
+                    if self.used + b.autotune_bytes() <= self.budget:
+                        tile, _ = b.autotune(report=False)
+                        if prec == "fp64":
+                            self.tile = tile
+                        self.zrange[prec] = b.zrange()
+                        self.tuned[prec] = True
+                    else:
+                        self.tune_skipped += 1
+                if prec == "fp64":
                     b.set_tile(self.tile if self.tile is not None else DEFAULT_TILE)
                 else:
                     b.set_tile(0)
+                if self.zrange[prec] is not None:
+                    b.set_zrange(self.zrange[prec])
                 self.batches[key] = b
                 self.batch_members[key] = list(rids)
                 self.batch_rebuilds += 1
 
     # -- one scheduling quantum --------------------------------------------
     def _launch(self) -> tuple[int, list]:
-        """Queue up to `quantum` steps for every simulation in a batch (no
-        wait); returns the steps queued and the requests that take them."""
+        """Queue up to `quantum` steps for every simulation in a batch, each
+        taking at most its remaining steps (no wait); returns the quantum and
+        the requests that take part."""
         members = [rid for rids in self.batch_members.values() for rid in rids]
         if not members:
             return 0, []
-        q = min(self.quantum, min(self.resident[rid].remaining for rid in members))
-        for b in self.batches.values():
-            b.steps(q)
+        q = min(self.quantum, max(self.resident[rid].remaining for rid in members))
+        for key, b in self.batches.items():
+            b.steps_limited(q, [self.resident[rid].remaining for rid in self.batch_members[key]])
         return q, members
 
     def _complete(self, q: int, members: list) -> None:
@@ -208,8 +232,9 @@ class Server:
             b.sync()
         for rid in members:
             r = self.resident[rid]
-            r.remaining -= q
-            self.cell_steps += r.req.case.cells * q
+            took = min(q, r.remaining)
+            r.remaining -= took
+            self.cell_steps += r.req.case.cells * took
 
     def run(self, requests: list, realtime: bool = True, virtual_step_s: float = 1e-3) -> dict:
         """Serve `requests`.  realtime=False replaces the wall clock by a
@@ -226,8 +251,15 @@ class Server:
         t0 = time.perf_counter()
         clock = (lambda: time.perf_counter() - t0) if realtime else None
         virtual = 0.0
+        next_report = self.progress_s
         while future or waiting or self.resident:
             now = clock() if realtime else virtual
+            if self.progress and now >= next_report:
+                next_report = now + self.progress_s
+                self.progress({"t_s": now, "completed": self.completed, "resident": len(self.resident),
+                               "waiting": len(waiting), "future": len(future), "cell_steps": self.cell_steps,
+                               "value": self.cell_steps / now if now > 0 else None,
+                               "batch_rebuilds": self.batch_rebuilds})
             while future and future[0].arrival <= now:
                 waiting.append(future.popleft())
             if self.policy == "srpt" and len(waiting) > 1:
@@ -266,7 +298,8 @@ class Server:
                 "value": self.cell_steps / wall if wall > 0 else None,
                 "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
                 "max_resident": self.max_resident, "batch_rebuilds": self.batch_rebuilds,
-                "tile": self.tile if self.tile is not None else DEFAULT_TILE}
+                "tile": self.tile if self.tile is not None else DEFAULT_TILE, "zrange": dict(self.zrange),
+                "tune_skipped": self.tune_skipped}
 
 
 def run_serial(requests: list, device_init: bool = True) -> dict:

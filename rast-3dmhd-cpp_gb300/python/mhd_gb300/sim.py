@@ -299,5 +299,25 @@ class Batch:
         for s in self.sims:
             s.timt += n * s.case.dt
 
+    def steps_limited(self, n: int, max_steps) -> None:
+        """n batched steps in which instance i takes only min(n, max_steps[i])."""
+        lim = (C.c_int * len(self.sims))(*[int(m) for m in max_steps])
+        abi.check(self.L.mhd_batch_steps_limited(self.b, n, lim))
+        for s, m in zip(self.sims, max_steps):
+            s.timt += min(n, int(m)) * s.case.dt
+
+    def set_zrange(self, zmax: int) -> None:
+        abi.check(self.L.mhd_batch_set_zrange(self.b, zmax))
+
+    def zrange(self) -> int:
+        z = C.c_int()
+        abi.check(self.L.mhd_batch_zrange(self.b, C.byref(z)))
+        return z.value
+
+    def autotune_bytes(self) -> int:
+        v = C.c_ulonglong()
+        abi.check(self.L.mhd_batch_autotune_bytes(self.b, C.byref(v)))
+        return v.value
+
     def sync(self) -> None:
         abi.check(self.L.mhd_batch_sync(self.b))

@@ -156,10 +156,11 @@ def config2_subset():
     return out
 
 
-@pytest.mark.parametrize("tile", [0, 2])
-def test_batch_config2_shapes_against_the_oracle(tile):
+@pytest.mark.parametrize("tile,zmax", [(0, 64), (2, 16)])
+def test_batch_config2_shapes_against_the_oracle(tile, zmax):
     """One batched step of config 2's real instance shapes, every instance
-    compared with the oracle directly: 1e-12 of each field's max-norm."""
+    compared with the oracle directly: 1e-12 of each field's max-norm.  With
+    zmax 16 every instance is split into 2 or 4 z ranges of one work list."""
     from gpu_util import oracle_for
     cases = config2_subset()
     assert any(c.nPz == 64 for c in cases) and any(c.nPx == 128 for c in cases)
@@ -172,6 +173,8 @@ def test_batch_config2_shapes_against_the_oracle(tile):
         sims.append(s)
     b = Batch(sims)
     b.set_tile(tile)
+    b.set_zrange(zmax)
+    assert b.zrange() == zmax
     b.steps(1)
     b.sync()
     got = [s.download_state() for s in sims]
@@ -183,3 +186,59 @@ def test_batch_config2_shapes_against_the_oracle(tile):
         o.steps(1)
         for k in STATE_FIELDS:
             assert rel_err(g[k], o.arr[k]) <= 1e-12, (c.nPx, c.nPz, k, rel_err(g[k], o.arr[k]))
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_limited_steps_equal_instances_alone(prec):
+    """mhd_batch_steps_limited: instance i takes min(n, limit[i]) of n batched
+    steps; each result equals the instance stepped alone that many times in a
+    batch of one (bit for bit), and a later unlimited call continues from it."""
+    cases = make_cases(seed0=80)[:4]
+    limits = [5, 0, 2, 7]
+
+    def fresh_p(c):
+        s = Simulation(c, path="fused", precision=prec)
+        s.upload_state(initial_state(c))
+        s.communicate()
+        return s
+    sims = [fresh_p(c) for c in cases]
+    b = Batch(sims)
+    b.set_tile(0)
+    b.steps_limited(5, limits)
+    b.steps(1)
+    b.sync()
+    got = [s.download_state() for s in sims]
+    b.close()
+    for s in sims:
+        s.close()
+    for i, c in enumerate(cases):
+        solo = fresh_p(c)
+        bs = Batch([solo])
+        bs.set_tile(0)
+        bs.steps(min(5, limits[i]) + 1)
+        bs.sync()
+        ref = solo.download_state()
+        bs.close()
+        solo.close()
+        for k in STATE_FIELDS:
+            assert np.array_equal(got[i][k], ref[k]), (prec, i, k)
+
+
+def test_fp32_autotune_picks_a_zrange():
+    cases = make_cases(seed0=100)
+
+    def fresh32(c):
+        s = Simulation(c, precision="fp32")
+        s.upload_state(initial_state(c))
+        s.communicate()
+        return s
+    sims = [fresh32(c) for c in cases]
+    b = Batch(sims)
+    assert b.autotune_bytes() > 0
+    chosen, ms = b.autotune()
+    assert chosen == 0 and ms[0] > 0 and b.zrange() in (64, 32, 16)
+    b.steps(1)
+    b.sync()
+    b.close()
+    for s in sims:
+        s.close()

@@ -69,6 +69,19 @@ class FakeBatch:
         for s in self.sims:
             s.steps_done += n
 
+    def steps_limited(self, n, limits):
+        for s, m in zip(self.sims, limits):
+            s.steps_done += min(n, m)
+
+    def autotune_bytes(self):
+        return 0
+
+    def zrange(self):
+        return 32
+
+    def set_zrange(self, z):
+        self.z = z
+
     def sync(self):
         pass
 
@@ -164,6 +177,27 @@ def test_srpt_admits_least_work_first_and_caps_resident_cells(fake_backend):
     assert fifo["policy"] == "fifo" and fifo["max_resident"] >= st["max_resident"]
 
 
+def test_server_skips_a_tuning_whose_scratch_does_not_fit(fake_backend, monkeypatch):
+    """The autotuner's scratch copy (24 doubles per cell here) counts against
+    the budget: one resident simulation fits, it and the copy do not."""
+    class SizedBatch(FakeBatch):
+        def autotune_bytes(self):
+            return sum(s.case.nx * s.case.ny * s.case.nz * 24 * 8 for s in self.sims)
+    monkeypatch.setattr(serve, "Batch", SizedBatch)
+
+    def stream():
+        reqs = poisson_requests(4, rate=50.0, seed=13, grid_min=(32, 32, 16), grid_max=(32, 32, 16), steps=(3, 8),
+                                fp32_fraction=0.0)
+        for r in reqs:
+            r.arrival = 0.0
+        return reqs
+    need = max(device_bytes_estimate(r.case, r.precision) for r in stream())
+    st = Server(need + (1 << 20), quantum=4, target_cells=1).run(stream(), realtime=False)
+    assert st["tune_skipped"] >= 1 and st["tile"] == serve.DEFAULT_TILE and st["zrange"]["fp64"] is None
+    st2 = Server(3 * need, quantum=4, target_cells=1).run(stream(), realtime=False)
+    assert st2["tune_skipped"] == 0 and st2["tile"] == 1 and st2["zrange"]["fp64"] == 32
+
+
 def test_scheduler_rejects_a_request_larger_than_the_budget(fake_backend):
     big = Request(rid=0, case=poisson_requests(1, 1.0, seed=2)[0].case, steps=3)
     with pytest.raises(RuntimeError):
@@ -217,3 +251,25 @@ def test_device_initial_state_mirror_is_a_seeded_gaussian():
     assert not np.array_equal(a["TT"], d["TT"])
     # periodic ghosts
     assert np.array_equal(a["TT"][:, 0, :], a["TT"][:, -2, :]) and np.array_equal(a["TT"][:, :, -1], a["TT"][:, :, 1])
+
+
+def test_quantum_does_not_shrink_to_the_shortest_request(fake_backend, monkeypatch):
+    """A request with one step left takes that step and drops out of the
+    quantum; the others still get the full quantum."""
+    calls = []
+
+    class RecordingBatch(FakeBatch):
+        def steps_limited(self, n, limits):
+            calls.append((n, list(limits)))
+            super().steps_limited(n, limits)
+    monkeypatch.setattr(serve, "Batch", RecordingBatch)
+    reqs = poisson_requests(2, rate=1e6, seed=2, grid_min=(16, 16, 8), grid_max=(16, 16, 8), steps=(3, 3),
+                            fp32_fraction=0.0)
+    reqs[0].steps, reqs[1].steps = 1, 50
+    for r in reqs:
+        r.arrival = 0.0
+    srv = Server(1 << 40, quantum=25, keep_results=True)
+    srv.run(reqs, realtime=False)
+    assert calls[0] == (25, [1, 50])
+    assert [n for n, _ in calls] == [25, 25]
+    assert [r.result["steps"] for r in reqs] == [1, 50]

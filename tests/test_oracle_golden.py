@@ -126,3 +126,21 @@ def test_config1_physics_64x64x32_20_steps_digest():
     sim.steps(d["steps"])
     for k in STATE_FIELDS:
         assert _sha(sim.arr[k]) == d["output_sha256"][k], k
+
+
+def test_threaded_cfl_reduction_equals_the_serial_one():
+    """The plane-parallel CFL reduction used by the CPU baseline's adaptive-dt
+    leg gives the serial (reference-order) DT and UMACH bit for bit on a
+    finite state."""
+    import oracle
+    from mhd_gb300.case import initial_state, small_cases
+    case = small_cases()["mhd_fixedT"]
+    st = initial_state(case)
+    o = oracle.OracleSim(case, st, nthreads=4)
+    o.communicate()
+    o.steps(2)
+    serial = o.cfl_dt()
+    o.p.cfl_parallel = 1
+    threaded = o.cfl_dt()
+    o.p.cfl_parallel = 0
+    assert serial == threaded

@@ -56,3 +56,24 @@ def test_realtime_poisson_run_reports_latency():
     st = srv.run(reqs, realtime=True)
     assert st["tts_p50_s"] > 0 and st["tts_p99_s"] >= st["tts_p50_s"]
     assert st["value"] > 0 and st["tile"] in (0, 1, 2)
+
+
+def test_autotuner_scratch_counts_against_the_budget():
+    """A budget that holds the simulations but not the autotuner's scratch
+    copy of their batch: the server skips the tuning and runs the default."""
+    reqs = poisson_requests(4, rate=50.0, seed=13, grid_min=(32, 32, 16), grid_max=(32, 32, 16), steps=(3, 8),
+                            fp32_fraction=0.0)
+    # target_cells=1: one simulation resident at a time, each fits alone but
+    # not beside the tuner's copy of it
+    need = max(device_bytes_estimate(r.case, r.precision) for r in reqs)
+    srv = Server(need + (1 << 20), quantum=4, target_cells=1, keep_results=False)
+    for r in reqs:
+        r.arrival = 0.0
+    st = srv.run(reqs, realtime=False)
+    assert st["tune_skipped"] >= 1 and st["tile"] == 2 and st["zrange"]["fp64"] is None
+    roomy = poisson_requests(4, rate=50.0, seed=13, grid_min=(32, 32, 16), grid_max=(32, 32, 16), steps=(3, 8),
+                             fp32_fraction=0.0)
+    for r in roomy:
+        r.arrival = 0.0
+    st2 = Server(3 * need, quantum=4, target_cells=1).run(roomy, realtime=False)
+    assert st2["tune_skipped"] == 0 and st2["zrange"]["fp64"] in (64, 32, 16)
