@@ -47,7 +47,7 @@ extern "C" {
 #define MHD_SW_LROT 0x1u
 #define MHD_SW_LMAG 0x2u
 #define MHD_SW_LPOT 0x4u /* no effect: the reference never reads lPot */
-#define MHD_SW_LREM 0x8u /* FP64 storage only; MHD_ERR_UNSUPPORTED with lShr or FP32 storage */
+#define MHD_SW_LREM 0x8u /* MHD_ERR_UNSUPPORTED with lShr; fused or parity path, FP64 or FP32 storage */
 #define MHD_SW_LSHR 0x10u
 
 /* storage precision of the state */

@@ -105,8 +105,6 @@ int validate(const mhd_params* p, std::string& why) {
     if ((p->switches & MHD_SW_LREM) && (p->switches & MHD_SW_LSHR))
         return why = "lRem with lShr: the reference's temperature terms then read arrays it did not fill this call (3dmhdsub.h:292-313)",
                MHD_ERR_UNSUPPORTED;
-    if ((p->switches & MHD_SW_LREM) && p->precision == MHD_PREC_FP32)
-        return why = "lRem runs on FP64 contexts only", MHD_ERR_UNSUPPORTED;
     if (p->izCon != 0 && p->izCon != 1) return why = "izCon must be 0 or 1", MHD_ERR_UNSUPPORTED;
     if (p->iTCon != 0 && p->iTCon != 1 && p->iTCon != 2 && p->iTCon != 4)
         return why = "iTCon must be 0, 1, 2 or 4", MHD_ERR_UNSUPPORTED;
@@ -352,6 +350,11 @@ int fused32_step(mhd_ctx* ctx, double dt, const double* dtp = nullptr) {
         a.gam = gam[s];
         a.zet = zet[s];
         a.substage = s;
+        if (ctx->c.lrem) {
+            // horizontal means of the substage's input T (3dmhdsub.h:297-313), in FP64
+            const int e = lrem_profiles32(ctx->g, ctx->c, a.U.p[S_TT], a.bgT, ctx->d_lrem, ctx->stream);
+            if (e) return cuda_fail(ctx, (cudaError_t)e, "lRem profiles launch");
+        }
         cudaEvent_t* ev = nullptr;
         if (ctx->profiling) {
             if (ctx->prof_used + 2 > ctx->prof_events.size()) {

@@ -119,6 +119,8 @@ int parity_communicate(int nf, const Grid& g, Fields8 U, cudaStream_t st);
 // `exact`, else by a parallel reduction), then HRAD and the fused form
 // G = HRAD - d2(TTM)/dz2, into buf = [TTM | HRAD | G] (3 x nz doubles).
 int lrem_profiles(const Grid& g, const Consts& c, const double* TT, double* buf, bool exact, cudaStream_t st);
+// HRAD and G from the plane means already in buf[0, nz) (buf as lrem_profiles)
+int lrem_hrad_from_means(const Grid& g, const Consts& c, double* buf, cudaStream_t st);
 // CFL partial minima/maxima; out[0..4] = UMACH^2-candidate max, w0..w3 minima.
 int parity_cfl(bool mag, const Grid& g, const Consts& c, Fields8 U, double* partials, int max_blocks,
                double* out5, cudaStream_t st);
@@ -206,6 +208,9 @@ int fused32_substage(unsigned sw, const Fused32Args& a, cudaStream_t st);
 int fused32_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const double* bgR,
                        const double* bgT, double timt, cudaStream_t st);
 int communicate32(int nf, const Grid& g, Fields8f U, cudaStream_t st);
+// lRem profiles (as lrem_profiles) of an FP32-storage temperature: the plane
+// means T0(z) + mean(dT) summed in FP64
+int lrem_profiles32(const Grid& g, const Consts& c, const float* dT, const double* bgT, double* buf, cudaStream_t st);
 // ragged batches of FP32-storage instances (tile 32x8; same item and counter
 // conventions as the FP64 batch)
 constexpr int kBatch32TX = 32, kBatch32TY = 8;

@@ -291,6 +291,16 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 const float lapT = D2x(F_DT) + D2y(F_DT) + (a.zf[4 * nzz + z] + D2z(F_DT));
                 ft = fmaf(ri * tmpc, fmaf(a.zf[5 * nzz + z], lapT, a.zf[6 * nzz + z] * Tz), ft);
             }
+            // lRem (3dmhdsub.h:297-313): conduction of T - TTM(z) plus HRAD, as
+            // lap T + G(z) with G = HRAD - d2 TTM/dz2 from the FP64 plane means;
+            // it replaces the kappa(z) conduction term above
+            if constexpr (EXTRA && !SW::lShr) {
+                if (c.lrem) {
+                    const float lapT = D2x(F_DT) + D2y(F_DT) + (a.zf[4 * nzz + z] + D2z(F_DT));
+                    ft = -fmaf(u, Dx(F_DT), fmaf(v, Dy(F_DT), w * Tz));
+                    ft = fmaf(ri * tmpc, lapT + (float)c.lrem_g[z], ft);
+                }
+            }
             // internal plume heat sink (iTCon 2, 3dmhdsub.h:443-459)
             if constexpr (EXTRA) {
                 if (c.pl_mode == 3)
@@ -482,7 +492,9 @@ __device__ __forceinline__ void bcon32_cell(const Grid& g, const Consts& c, cons
                  c.C23 * DZ * (c.THETA - (c.THETA - c.pl_tpr) * c.plx[x] / c.pl_hh * c.ply[y] / c.pl_hh);
         } else if (c.iTCon == 1) {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
-            tt = c.C43 * t1 - c.C13 * t2 - c.C23 * DZ * c.THETA;
+            tt = c.lrem ? c.C43 * t1 - c.C13 * t2 + c.DZTU : c.C43 * t1 - c.C13 * t2 - c.C23 * DZ * c.THETA;
+        } else if (c.lrem) {
+            tt = c.TU;
         } else {
             tt = 1.0;
             if (c.iTCon == 4 && x < g.nx / 2) tt = 1.0f - c.TP;
@@ -490,6 +502,8 @@ __device__ __forceinline__ void bcon32_cell(const Grid& g, const Consts& c, cons
     } else {
         if (c.izCon == 0) {
             tt = c.TB;
+        } else if (c.lrem) {
+            tt = c.C43 * t1 - c.C13 * t2 + c.DZTB;
         } else {
             const double DZ = 1.0f / (float)(g.nPz - 1) / c.dzzdz[z];
             tt = c.C43 * t1 - c.C13 * t2 - c.C23 * DZ * c.THETA / c.RKAPA[z];
@@ -601,7 +615,7 @@ void launch32_t(const Fused32Args& a, cudaStream_t st, int* rc) {
 
 template <class SW>
 void launch32(const Fused32Args& a, cudaStream_t st, int* rc) {
-    if (a.c.pl_mode == 3) launch32_t<SW, true>(a, st, rc);
+    if (a.c.pl_mode == 3 || a.c.lrem) launch32_t<SW, true>(a, st, rc);
     else launch32_t<SW, false>(a, st, rc);
 }
 
@@ -662,6 +676,36 @@ int fused32_bcon_ghost(unsigned sw, const Grid& g, const Consts& c, Fields8f U, 
                        const double* bgT, double timt, cudaStream_t st) {
     MHD_DISPATCH_SW(sw, launch_bcon32, g, c, U, Z, bgR, bgT, timt, st);
     return (int)cudaGetLastError();
+}
+
+namespace {
+
+// plane means of T = T0(z) + dT over the interior (y, x), the deviations summed
+// in FP64 by a block reduction per plane
+__global__ void k_lrem_ttm32(Grid g, const float* dT, const double* bgT, double* ttm) {
+    __shared__ double s[256];
+    const int z = blockIdx.x;
+    const int n = (g.nx - 2) * (g.ny - 2);
+    double w = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int y = 1 + k / (g.nx - 2), x = 1 + k % (g.nx - 2);
+        w += (double)dT[(long long)z * g.sz + (long long)y * g.sy + x];
+    }
+    s[threadIdx.x] = w;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) ttm[z] = bgT[z] + s[0] / (double)n;
+}
+
+}  // namespace
+
+int lrem_profiles32(const Grid& g, const Consts& c, const float* dT, const double* bgT, double* buf, cudaStream_t st) {
+    k_lrem_ttm32<<<g.nz, 256, 0, st>>>(g, dT, bgT, buf);
+    const int e = (int)cudaGetLastError();
+    return e ? e : lrem_hrad_from_means(g, c, buf, st);
 }
 
 int communicate32(int nf, const Grid& g, Fields8f U, cudaStream_t st) {

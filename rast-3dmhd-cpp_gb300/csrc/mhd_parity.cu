@@ -1030,6 +1030,11 @@ int cfl_dt_on_device(bool mag, const Grid& g, const Consts& c, Fields8 U, double
     return (int)cudaGetLastError();
 }
 
+int lrem_hrad_from_means(const Grid& g, const Consts& c, double* buf, cudaStream_t st) {
+    k_lrem_hrad<<<(g.nz + 63) / 64, 64, 0, st>>>(g, c, buf, buf + g.nz, buf + 2 * g.nz);
+    return (int)cudaGetLastError();
+}
+
 int lrem_profiles(const Grid& g, const Consts& c, const double* TT, double* buf, bool exact, cudaStream_t st) {
     double *ttm = buf, *hrad = buf + g.nz, *G = buf + 2 * g.nz;
     if (exact) k_lrem_ttm_exact<<<(g.nz + 63) / 64, 64, 0, st>>>(g, TT, ttm);

@@ -62,13 +62,11 @@ def test_invalid_configs_rejected_without_gpu(lib, change, status):
 
 
 def test_lrem_and_nonperiodic_rejected(lib):
-    """lRem with lShr (the reference then reads unfilled arrays) and lRem in
-    FP32 storage are rejected, as are non-periodic horizontal walls."""
+    """lRem with lShr (the reference then reads unfilled arrays) is rejected,
+    as are non-periodic horizontal walls."""
     case = small_cases()["mhd_rot_shr"].replace(lRem=True)
     p, keep = params_for(case)
     ctx = C.c_void_p()
-    assert lib.mhd_create(C.byref(p), None, C.byref(ctx)) == -2
-    p, keep = params_for(small_cases()["mhd_fixedT"].replace(lRem=True), precision="fp32")
     assert lib.mhd_create(C.byref(p), None, C.byref(ctx)) == -2
     case = small_cases()["mhd_fixedT"]
     p, keep = params_for(case)

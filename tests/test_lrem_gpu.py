@@ -59,3 +59,34 @@ def test_lrem_batches_rejected():
     with pytest.raises(abi.MhdError):
         Batch([sim])
     sim.close()
+
+
+@pytest.mark.parametrize("name", lrem_case_names())
+def test_fp32_storage_within_precision_tolerance(name):
+    """lRem with FP32 field storage (FP64 plane means, RK register and
+    equation of state): 3 steps against the reference's fixture within the
+    precision form's 1e-5 (relative L2 and max-norm), and its first CFL dt
+    within 1e-6 of the reference's."""
+    from gpu_util import METRIC_NAMES
+    case, g = load_golden(name)
+    mo = {n: g["in_" + n] for n in METRIC_NAMES}
+
+    def fresh():
+        s = Simulation(case, path="fused", precision="fp32", metric_override=mo)
+        s.upload_state({k: g["in_" + k] for k in STATE_FIELDS})
+        s.communicate()
+        return s
+    sim = fresh()
+    for _ in range(3):
+        sim.step(case.dt)
+    got = sim.download_state()
+    sim.close()
+    for k in STATE_FIELDS[:case.nfields]:
+        a, b = got[k][1:-1, 1:-1, 1:-1], g["steps3_" + k][1:-1, 1:-1, 1:-1]
+        nb = np.linalg.norm(b)
+        l2 = np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+        assert l2 <= 1e-5 and rel_err(got[k], g["steps3_" + k]) <= 1e-5, (k, l2)
+    sim = fresh()
+    _, d = sim.steps_cfl(1)
+    assert abs(d["dt"] / g["cfl2_dt"][0] - 1.0) <= 1e-6
+    sim.close()
