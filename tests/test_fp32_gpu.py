@@ -82,6 +82,30 @@ def test_config0_200_steps_l2_error(capsys):
     assert abs(res["fp32"][1]["total_mass"] / res["fp64"][1]["total_mass"] - 1) < 1e-8
 
 
+def test_config3_1000_steps_l2_error(capsys):
+    """The precision configuration at its stated size: 256x256x128 MHD, noise
+    1e-2, 1000 steps with FP32 storage against the FP64 fused path (itself
+    within 1e-12 of the oracle per step); every field within 1e-5 relative
+    L2, and the total mass of both within 1e-8."""
+    from mhd_gb300.case import config3
+    case = config3()
+    st = initial_state(case)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        sim = Simulation(case, precision=prec)
+        sim.upload_state(st)
+        sim.communicate()
+        sim.steps(1000, case.dt)
+        res[prec] = (sim.download_state(), sim.diagnostics())
+        sim.close()
+    errs = {k: l2_rel(res["fp32"][0][k], res["fp64"][0][k]) for k in STATE_FIELDS}
+    with capsys.disabled():
+        print("\nFP32-storage vs FP64, 256x256x128, 1000 steps, relative L2:", {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v <= 1e-5, (k, v)
+    assert abs(res["fp32"][1]["total_mass"] / res["fp64"][1]["total_mass"] - 1) < 1e-8
+
+
 def test_cfl_and_diagnostics_fp32():
     case = small_cases()["mhd_fixedT"]
     st = initial_state(case)
