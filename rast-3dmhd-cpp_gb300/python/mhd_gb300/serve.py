@@ -121,7 +121,8 @@ class Server:
 
     def __init__(self, hbm_budget_bytes: int, quantum: int = 25, tile: int | None = None,
                  keep_results: bool = False, device_init: bool = True, policy: str = "srpt",
-                 target_cells: int = 64_000_000, progress=None, progress_s: float = 30.0):
+                 target_cells: int = 64_000_000, progress=None, progress_s: float = 30.0,
+                 balance: bool = True, rates: dict | None = None):
         if policy not in ("fifo", "srpt"):
             raise ValueError(f"unknown admission policy {policy!r}")
         self.policy = policy
@@ -132,6 +133,9 @@ class Server:
         self.tile = tile
         self.tuned = {"fp64": tile is not None, "fp32": False}
         self.zrange = {"fp64": None, "fp32": None}
+        self.balance = balance
+        # nominal cell-RK3-updates/s of a batch per precision (measured, 64-instance batch)
+        self.rates = dict(rates or {"fp64": 7.9e8, "fp32": 3.0e9})
         self.progress = progress
         self.progress_s = float(progress_s)
         self.completed = 0
@@ -214,27 +218,56 @@ class Server:
                 self.batch_rebuilds += 1
 
     # -- one scheduling quantum --------------------------------------------
-    def _launch(self) -> tuple[int, list]:
-        """Queue up to `quantum` steps for every simulation in a batch, each
-        taking at most its remaining steps (no wait); returns the quantum and
-        the requests that take part."""
-        members = [rid for rids in self.batch_members.values() for rid in rids]
-        if not members:
-            return 0, []
-        q = min(self.quantum, max(self.resident[rid].remaining for rid in members))
-        for key, b in self.batches.items():
-            b.steps_limited(q, [self.resident[rid].remaining for rid in self.batch_members[key]])
-        return q, members
+    def _quanta(self) -> dict:
+        """Steps per batch for the next quantum.  The batch with the longest
+        estimated step (cells / nominal rate of its precision) takes `quantum`
+        steps; with balance on, every other batch takes as many steps as fit
+        in the same time (at most 8 x quantum), so the FP32-storage batch,
+        about four times faster per cell, does not idle while the FP64 batch
+        finishes its quantum."""
+        est = {key: sum(self.resident[rid].req.case.cells for rid in rids) / self.rates[key[0]]
+               for key, rids in self.batch_members.items()}
+        longest = max(est.values())
+        out = {}
+        for key, rids in self.batch_members.items():
+            q = self.quantum
+            if self.balance and est[key] > 0:
+                q = int(min(8 * self.quantum, max(self.quantum, round(self.quantum * longest / est[key]))))
+            out[key] = min(q, max(self.resident[rid].remaining for rid in rids))
+        return out
 
-    def _complete(self, q: int, members: list) -> None:
-        """Wait for the queued quantum and account its steps."""
+    def _launch(self) -> tuple[dict, dict]:
+        """Queue each batch's quantum, every simulation taking at most its
+        remaining steps (no wait); returns the steps per batch and the
+        requests of each batch."""
+        if not self.batch_members:
+            return {}, {}
+        qs = self._quanta()
+        members = {key: list(rids) for key, rids in self.batch_members.items()}
+        for key, b in self.batches.items():
+            b.steps_limited(qs[key], [self.resident[rid].remaining for rid in members[key]])
+        return qs, members
+
+    def _complete(self, qs: dict, members: dict) -> int:
+        """Wait for the queued quantum and account its steps; returns the steps
+        taken by the batch whose quantum was estimated to take longest (the
+        virtual clock's measure of the quantum)."""
         for b in self.batches.values():
             b.sync()
-        for rid in members:
-            r = self.resident[rid]
-            took = min(q, r.remaining)
-            r.remaining -= took
-            self.cell_steps += r.req.case.cells * took
+        longest, steps = -1.0, 0
+        for key, rids in members.items():
+            took_cells, took_max = 0, 0
+            for rid in rids:
+                r = self.resident[rid]
+                took = min(qs[key], r.remaining)
+                r.remaining -= took
+                self.cell_steps += r.req.case.cells * took
+                took_cells += r.req.case.cells * took
+                took_max = max(took_max, took)
+            t = took_cells / self.rates[key[0]]
+            if t > longest:
+                longest, steps = t, took_max
+        return steps
 
     def run(self, requests: list, realtime: bool = True, virtual_step_s: float = 1e-3) -> dict:
         """Serve `requests`.  realtime=False replaces the wall clock by a
@@ -264,7 +297,7 @@ class Server:
                 waiting.append(future.popleft())
             if self.policy == "srpt" and len(waiting) > 1:
                 waiting = deque(sorted(waiting, key=lambda r: (r.case.cells * r.steps, r.arrival)))
-            q, members = self._launch()
+            qs, members = self._launch()
             changed = False
             while waiting and self._admit(waiting[0], now):
                 waiting.popleft()
@@ -280,9 +313,9 @@ class Server:
                         virtual = nxt
                 continue
             if members:
-                self._complete(q, members)
+                took = self._complete(qs, members)
                 if not realtime:
-                    virtual += q * virtual_step_s
+                    virtual += took * virtual_step_s
             now = clock() if realtime else virtual
             done = [r for r in self.resident.values() if r.remaining <= 0]
             for r in done:

@@ -273,3 +273,32 @@ def test_quantum_does_not_shrink_to_the_shortest_request(fake_backend, monkeypat
     assert calls[0] == (25, [1, 50])
     assert [n for n, _ in calls] == [25, 25]
     assert [r.result["steps"] for r in reqs] == [1, 50]
+
+
+def test_quanta_balance_the_precisions(fake_backend, monkeypatch):
+    """With balance on, a batch whose steps are estimated to take a quarter
+    of the time takes four times the steps per quantum (capped at 8 x
+    quantum); without it every batch takes the quantum."""
+    calls = []
+
+    class RecordingBatch(FakeBatch):
+        def steps_limited(self, n, limits):
+            calls.append((self.sims[0].precision, n))
+            super().steps_limited(n, limits)
+    monkeypatch.setattr(serve, "Batch", RecordingBatch)
+
+    def stream():
+        reqs = poisson_requests(2, rate=1e6, seed=2, grid_min=(16, 16, 8), grid_max=(16, 16, 8), steps=(3, 3))
+        reqs[0].precision, reqs[1].precision = "fp64", "fp32"
+        for r in reqs:
+            r.steps, r.arrival = 400, 0.0
+        return reqs
+    srv = Server(1 << 40, quantum=10, rates={"fp64": 1.0, "fp32": 4.0}, keep_results=True)
+    reqs = stream()
+    srv.run(reqs, realtime=False)
+    first = dict(calls[:2])
+    assert first == {"fp64": 10, "fp32": 40}
+    assert [r.result["steps"] for r in reqs] == [400, 400]
+    calls.clear()
+    Server(1 << 40, quantum=10, balance=False).run(stream(), realtime=False)
+    assert dict(calls[:2]) == {"fp64": 10, "fp32": 10}
