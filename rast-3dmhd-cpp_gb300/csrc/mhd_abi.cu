@@ -264,8 +264,13 @@ int profiles_from_means(mhd_ctx* ctx) {
         ctx->h_zf[3 * (size_t)nz + z] = (float)ctx->h_bg[2 * (size_t)nz + z];
         ctx->h_zf[4 * (size_t)nz + z] = (float)ctx->h_bg[3 * (size_t)nz + z];
     }
-    CK(cudaMemcpy(ctx->d_bg, ctx->h_bg.data(), sizeof(double) * 4 * nz, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz, cudaMemcpyHostToDevice));
+    // on the context's stream: its kernels read the profiles (a plain cudaMemcpy
+    // runs on the legacy stream, which the non-blocking context stream does not
+    // wait for); the sync keeps h_bg / h_zf stable until the copies are done
+    CK(cudaMemcpyAsync(ctx->d_bg, ctx->h_bg.data(), sizeof(double) * 4 * nz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return MHD_OK;
 }
 }  // namespace mhd::ctxops
@@ -281,11 +286,12 @@ int upload32(mhd_ctx* ctx, int field, const double* host) {
     const size_t plane = (size_t)ctx->g.sz;
     std::vector<float> tmp(ctx->ncell);
     for (size_t i = 0; i < ctx->ncell; i++) tmp[i] = (float)(host[i] - (bg ? bg[i / plane] : 0.0));
-    CK(cudaStreamSynchronize(ctx->stream));
-    CK(cudaMemcpy(ctx->U32[ctx->cur] + (size_t)field * ctx->ncell, tmp.data(), ctx->ncell * sizeof(float),
-                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(ctx->U32[ctx->cur] + (size_t)field * ctx->ncell, tmp.data(), ctx->ncell * sizeof(float),
+                       cudaMemcpyHostToDevice, ctx->stream));
     // the FP64 register carries the full state between steps
-    CK(cudaMemcpy(ctx->Zb + (size_t)field * ctx->ncell, host, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(ctx->Zb + (size_t)field * ctx->ncell, host, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // tmp and the caller's array may go away after return
     ctx->ghosts_synced = false;
     return MHD_OK;
 }
@@ -402,7 +408,8 @@ int mhd_set_plume(mhd_ctx* ctx, const mhd_plume* pl) {
     for (int x = 0; x < nx; x++) h[x] = sink ? std::exp(CLN * sq(pl->EXX[x] - pl->XP) / HH) : std::exp(CLN * sq(pl->EXX[x] - pl->XP));
     for (int y = 0; y < ny; y++) h[nx + y] = sink ? std::exp(CLN * sq(pl->WYY[y] - pl->YP) / HH) : std::exp(CLN * sq(pl->WYY[y] - pl->YP));
     for (int z = 0; z < nz; z++) h[nx + ny + z] = std::exp(CLN * sq(pl->ZEE[z] - pl->ZP) / HH);
-    CK(cudaMemcpy(ctx->d_plume, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(ctx->d_plume, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     ctx->c.plx = ctx->d_plume;
     ctx->c.ply = ctx->d_plume + nx;
     ctx->c.plz = ctx->d_plume + nx + ny;
@@ -618,7 +625,8 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         lapZ_off[2 * k + 1] = push_z([&](int z) { return zb(z) - za(z); });
     }
     if (cudaMalloc(&ctx->d_metric, h.size() * sizeof(double)) != cudaSuccess ||
-        cudaMemcpy(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpyAsync(ctx->d_metric, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream) !=
+            cudaSuccess) {
         cudaGetLastError();
         mhd_destroy(ctx);
         return MHD_ERR_NOMEM;
@@ -674,15 +682,15 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
         arc = alloc_f32(ctx, &ctx->U32[0]);
         // 4 x nz double profiles, then the [7][nz] float coefficient table (8 x nz doubles in all)
         if (!arc && cudaMalloc(&ctx->d_bg, sizeof(double) * 8 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
-        if (!arc && cudaMemset(ctx->d_bg, 0, sizeof(double) * 8 * nz) != cudaSuccess) arc = MHD_ERR_CUDA;
+        if (!arc && cudaMemsetAsync(ctx->d_bg, 0, sizeof(double) * 8 * nz, ctx->stream) != cudaSuccess) arc = MHD_ERR_CUDA;
         ctx->h_zf.assign(7 * (size_t)nz, 0.0f);
         for (int z = 0; z < nz; z++) {
             for (int r = 0; r < 3; r++) ctx->h_zf[(size_t)r * nz + z] = (float)ctx->h_cz[(size_t)r * nz + z];
             ctx->h_zf[5 * (size_t)nz + z] = (float)p.RKAPA[z];
             ctx->h_zf[6 * (size_t)nz + z] = (float)p.DKAPA[z];
         }
-        if (!arc && cudaMemcpy(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz,
-                               cudaMemcpyHostToDevice) != cudaSuccess) arc = MHD_ERR_CUDA;
+        if (!arc && cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 7 * nz,
+                                    cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) arc = MHD_ERR_CUDA;
     } else {
         arc = alloc_block(ctx, &ctx->U[0], 8);
     }
@@ -710,6 +718,14 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     ctx->bytes += sizeof(double) * (8 * (size_t)ctx->red_blocks + 8 + kDtRecord);
     ctx->timt = ctx->timi = ctx->timc = 0.0;
     ctx->nit = 0;
+    // the uploads and clears above are ordered on the context's stream; finish
+    // them before the host tables go away and before other streams read them
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        fprintf(stderr, "mhd_create: the set-up copies failed\n");
+        mhd_destroy(ctx);
+        return MHD_ERR_CUDA;
+    }
     *out = ctx;
     return MHD_OK;
 }

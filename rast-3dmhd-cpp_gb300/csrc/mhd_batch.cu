@@ -41,6 +41,7 @@ struct mhd_batch {
     bool uxy = true;   // every instance has uniform x/y grids
     bool fp32 = false; // FP32-storage instances (one tile shape, 32x8)
     int* d_left = nullptr;       // [n] steps each instance still takes in the current call
+    int* d_err = nullptr;        // [4] the kernels' item checks (BatchCtl::err)
     int* h_left = nullptr;       // pinned staging of d_left
     cudaEvent_t left_copied = nullptr;  // the last copy of h_left has been read
     Fused32Args* d_args32 = nullptr;  // [2][3][n] for FP32 batches
@@ -186,6 +187,33 @@ void make_items(const mhd_batch* b, int tile, int zmax, std::vector<int4>& items
     });
 }
 
+// The kernels' item checks (batch_item_ok) on the host, before any capture:
+// a malformed work list is reported as an error instead of being launched.
+int check_items(mhd_batch* b, int tile, const std::vector<int4>& items) {
+    int tx, ty;
+    if (b->fp32) {
+        tx = kBatch32TX;
+        ty = kBatch32TY;
+    } else {
+        batch_tile_dims(tile, &tx, &ty);
+    }
+    const int n = (int)b->ctx.size();
+    for (const int4& it : items) {
+        const int zb = it.w & 0xffff, ze = it.w >> 16;
+        bool ok = it.x >= 0 && it.x < n;
+        if (ok) {
+            const Grid& g = b->ctx[it.x]->g;
+            ok = it.y >= 0 && it.z >= 0 && 1 + it.y * tx <= g.nx - 2 && 1 + it.z * ty <= g.ny - 2 && zb >= 1 &&
+                 ze <= g.nz - 1 && zb < ze;
+        }
+        if (!ok)
+            return bfail(b, MHD_ERR_INVALID, "malformed work item (instance " + std::to_string(it.x) + ", tile " +
+                                                 std::to_string(it.y) + "," + std::to_string(it.z) + ", z " +
+                                                 std::to_string(zb) + ".." + std::to_string(ze) + ")");
+    }
+    return MHD_OK;
+}
+
 void make_bcon_items(const mhd_batch* b, std::vector<int2>& items) {
     items.clear();
     for (size_t i = 0; i < b->ctx.size(); i++) {
@@ -211,6 +239,7 @@ int capture(mhd_batch* b, int tile, const FusedArgs* d_args, const Fused32Args* 
             int* d_counters, cudaGraphExec_t out[2]) {
     const int n = (int)b->ctx.size();
     const int grid = persistent_grid(b, tile, nitems);
+    const BatchCtl ctl{b->d_left, b->d_err, n};
     for (int p = 0; p < 2; p++) {
         cudaGraph_t graph;
         BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -219,17 +248,17 @@ int capture(mhd_batch* b, int tile, const FusedArgs* d_args, const Fused32Args* 
         for (int s = 0; s < 3 && !rc; s++) {
             if (b->fp32) {
                 const Fused32Args* a32 = d_args32 + ((size_t)p * 3 + s) * n;
-                rc = fused32_batch_substage(b->sw, a32, d_items, nitems, d_counters + 3 * p + s, b->d_left, grid,
+                rc = fused32_batch_substage(b->sw, a32, d_items, nitems, d_counters + 3 * p + s, ctl, grid,
                                             b->stream);
-                if (!rc) rc = fused32_batch_bcon(b->sw, a32, b->d_bitems, b->d_left, b->nbitems, b->stream);
+                if (!rc) rc = fused32_batch_bcon(b->sw, a32, b->d_bitems, ctl, b->nbitems, b->stream);
                 continue;
             }
             const FusedArgs* args = d_args + ((size_t)p * 3 + s) * n;
             rc = b->uxy ? fused_batch_substage_uxy(b->sw, tile, args, d_items, nitems, d_counters + 3 * p + s,
-                                                   b->d_left, grid, b->stream)
+                                                   ctl, grid, b->stream)
                         : fused_batch_substage_gen(b->sw, tile, args, d_items, nitems, d_counters + 3 * p + s,
-                                                   b->d_left, grid, b->stream);
-            if (!rc) rc = fused_batch_bcon(b->sw, args, b->d_bitems, b->d_left, b->nbitems, b->stream);
+                                                   ctl, grid, b->stream);
+            if (!rc) rc = fused_batch_bcon(b->sw, args, b->d_bitems, ctl, b->nbitems, b->stream);
         }
         if (!rc) rc = batch_tick(b->d_left, n, b->stream);
         const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
@@ -284,17 +313,25 @@ int build(mhd_batch* b) {
         }
         std::vector<Fused32Args> a32;
         fill_args32(b, V0, V1, Z32, FT32, cur, a32);
-        BCK(cudaMemcpy(b->d_args32, a32.data(), sizeof(Fused32Args) * a32.size(), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpyAsync(b->d_args32, a32.data(), sizeof(Fused32Args) * a32.size(), cudaMemcpyHostToDevice,
+                            b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
     } else {
         std::vector<FusedArgs> args;
         fill_args(b, U0, U1, Z, FT, cur, args);
-        BCK(cudaMemcpy(b->d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpyAsync(b->d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
     }
     std::vector<int4> items;
     make_items(b, b->tile, b->zmax, items);
+    if (int rc = check_items(b, b->tile, items)) return rc;
     cudaFree(b->d_items);
     BCK(cudaMalloc(&b->d_items, sizeof(int4) * items.size()));
-    BCK(cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    // on the batch's stream, which the graphs run on: a plain cudaMemcpy runs on
+    // the legacy stream, which the non-blocking batch stream does not wait for,
+    // and its DMA may still be in flight when it returns
+    BCK(cudaMemcpyAsync(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
     b->nitems = (int)items.size();
     drop_graphs(b->exec);
     int rc = capture(b, b->tile, b->d_args, b->d_args32, b->d_items, b->nitems, b->d_counters, b->exec);
@@ -370,11 +407,13 @@ int autotune(mhd_batch* b, double* ms_out) {
         if (b->fp32) {
             std::vector<Fused32Args> a32;
             fill_args32(b, V0, V1, Z, FT, cur, a32);
-            cudaMemcpy(d_args32, a32.data(), sizeof(Fused32Args) * a32.size(), cudaMemcpyHostToDevice);
+            cudaMemcpyAsync(d_args32, a32.data(), sizeof(Fused32Args) * a32.size(), cudaMemcpyHostToDevice, b->stream);
+            cudaStreamSynchronize(b->stream);
         } else {
             std::vector<FusedArgs> args;
             fill_args(b, U0, U1, Z, FT, cur, args);
-            cudaMemcpy(d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice);
+            cudaMemcpyAsync(d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice, b->stream);
+            cudaStreamSynchronize(b->stream);
         }
         // every instance steps in every timed step
         for (int i = 0; i < n; i++) b->h_left[i] = kNoLimit;
@@ -390,12 +429,14 @@ int autotune(mhd_batch* b, double* ms_out) {
             const int t = cand % ntiles, zc = cand / ntiles;
             std::vector<int4> items;
             make_items(b, t, kZMax[zc], items);
+            if ((rc = check_items(b, t, items))) break;
             int4* d_items = nullptr;
             if (cudaMalloc(&d_items, sizeof(int4) * items.size()) != cudaSuccess) {
                 rc = MHD_ERR_NOMEM;
                 break;
             }
-            cudaMemcpy(d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice);
+            cudaMemcpyAsync(d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, b->stream);
+            cudaStreamSynchronize(b->stream);
             cudaGraphExec_t ex[2] = {nullptr, nullptr};
             rc = capture(b, t, d_args, d_args32, d_items, (int)items.size(), d_cnt, ex);
             if (!rc) {
@@ -485,8 +526,12 @@ int mhd_batch_create(mhd_ctx* const* ctxs, const double* dts, int n, void* strea
         cudaMalloc(&b->d_args32, sizeof(Fused32Args) * 6 * n) != cudaSuccess ||
         cudaMalloc(&b->d_counters, sizeof(int) * 6) != cudaSuccess ||
         cudaMalloc(&b->d_bitems, sizeof(int2) * bitems.size()) != cudaSuccess ||
-        cudaMemcpy(b->d_bitems, bitems.data(), sizeof(int2) * bitems.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_bitems, bitems.data(), sizeof(int2) * bitems.size(), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
         cudaMalloc(&b->d_left, sizeof(int) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_err, sizeof(int) * 4) != cudaSuccess ||
+        cudaMemsetAsync(b->d_err, 0, sizeof(int) * 4, b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess ||
         cudaMallocHost(&b->h_left, sizeof(int) * n) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->left_copied, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
@@ -509,6 +554,7 @@ int mhd_batch_destroy(mhd_batch* b) {
     cudaFree(b->d_bitems);
     cudaFree(b->d_counters);
     cudaFree(b->d_left);
+    cudaFree(b->d_err);
     if (b->h_left) cudaFreeHost(b->h_left);
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -633,6 +679,15 @@ int mhd_batch_steps_limited(mhd_batch* b, int nsteps, const int* max_steps) {
 int mhd_batch_sync(mhd_batch* b) {
     if (!b) return MHD_ERR_INVALID;
     BCK(cudaStreamSynchronize(b->stream));
+    // the kernels' work-item checks: a failed item was skipped, not stepped
+    int e[4] = {0, 0, 0, 0};
+    BCK(cudaMemcpy(e, b->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e[0])
+        return bfail(b, MHD_ERR_INVALID,
+                     "a work item failed its check (code " + std::to_string(e[0]) + ", instance " +
+                         std::to_string(e[1]) + ", tile " + std::to_string(e[2] & 0xffff) + "," +
+                         std::to_string(e[2] >> 16) + ", z " + std::to_string(e[3] & 0xffff) + ".." +
+                         std::to_string(e[3] >> 16) + ") and was skipped");
     return MHD_OK;
 }
 

@@ -164,16 +164,59 @@ int fused_substage_xp(unsigned sw, const FusedArgs& a, cudaStream_t st);
 // counter that must be zero at launch.  Tile shapes: 0 = 32x4, 1 = 32x8, 2 = 16x8.
 constexpr int kBatchTiles = 3;
 void batch_tile_dims(int tile, int* tx, int* ty);
+// Per-call control of a ragged batch (device pointers): left[i] = the steps
+// instance i still takes in this call (its items are skipped at 0); err[0] =
+// the first failed item check (0 = none), err[1..3] = that item (instance,
+// tile x | tile y << 16, z range); n = the number of instances.
+struct BatchCtl {
+    int* left;
+    int* err;
+    int n;
+};
+
+// Check of a work item and of its instance's arguments before a kernel uses
+// them: an item that fails records its code in ctl.err and is skipped, so a
+// malformed work list shows up as an error status instead of a stray access.
+// Codes: 1 instance index, 2 grid sizes, 3 tile position, 4 z range, 5 a
+// field pointer is null.
+template <class A>
+__device__ __forceinline__ bool batch_item_ok(const BatchCtl& ctl, const A* args, int4 it, int tx, int ty, int nf) {
+    int code = 0;
+    if (it.x < 0 || it.x >= ctl.n) {
+        code = 1;
+    } else {
+        const A& a = args[it.x];
+        const int zb = it.w & 0xffff, ze = it.w >> 16;
+        if (a.g.nx < 3 || a.g.ny < 3 || a.g.nz < 6 || a.g.sy != a.g.nx || a.g.sz != (long long)a.g.nx * a.g.ny)
+            code = 2;
+        else if (it.y < 0 || it.z < 0 || 1 + it.y * tx > a.g.nx - 2 || 1 + it.z * ty > a.g.ny - 2)
+            code = 3;
+        else if (zb < 1 || ze > a.g.nz - 1 || zb >= ze)
+            code = 4;
+        else
+            for (int f = 0; f < nf; f++)
+                if (!a.U.p[f] || !a.Uo.p[f] || !a.Z.p[f]) code = 5;
+    }
+    if (code) {
+        if (atomicCAS(ctl.err, 0, code) == 0) {
+            ctl.err[1] = it.x;
+            ctl.err[2] = it.y | (it.z << 16);
+            ctl.err[3] = it.w;
+        }
+        return false;
+    }
+    return true;
+}
+
 // _uxy: uniform x/y grids (d2xxdx2 = d2yydy2 = 0); _gen: any grid.
-// Item w = first z plane | (end plane << 16).  left[i] (device, one per
-// instance): the steps instance i still takes; its items are skipped at 0.
+// Item w = first z plane | (end plane << 16).
 int fused_batch_substage_uxy(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
-                             const int* left, int grid, cudaStream_t st);
+                             BatchCtl ctl, int grid, cudaStream_t st);
 int fused_batch_substage_gen(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems, int* counter,
-                             const int* left, int grid, cudaStream_t st);
+                             BatchCtl ctl, int grid, cudaStream_t st);
 int fused_batch_occupancy_uxy(unsigned sw, int tile, int* blocks_per_sm);
 int fused_batch_occupancy_gen(unsigned sw, int tile, int* blocks_per_sm);
-int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, const int* left, int nblocks,
+int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, BatchCtl ctl, int nblocks,
                      cudaStream_t st);
 // end of a batched step: left[i] -= 1 where positive
 int batch_tick(int* left, int n, cudaStream_t st);
@@ -215,9 +258,9 @@ int lrem_profiles32(const Grid& g, const Consts& c, const float* dT, const doubl
 // conventions as the FP64 batch)
 constexpr int kBatch32TX = 32, kBatch32TY = 8;
 int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter,
-                           const int* left, int grid, cudaStream_t st);
+                           BatchCtl ctl, int grid, cudaStream_t st);
 int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm);
-int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, const int* left, int nblocks,
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, BatchCtl ctl, int nblocks,
                        cudaStream_t st);
 // CFL reduction of an FP32-storage state (the FP64 row kernel on the widened
 // fields): out5 as parity_cfl, or the device time-step record as cfl_dt_on_device

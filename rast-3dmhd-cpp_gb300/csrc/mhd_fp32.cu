@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_substage32(Fused32Args a) {
 template <class SW>
 __global__ void __launch_bounds__(kThreads, 3) k_substage32_batch(const Fused32Args* __restrict__ args,
                                                                const int4* __restrict__ items, int nitems,
-                                                               int* counter, const int* __restrict__ left) {
+                                                               int* counter, BatchCtl ctl) {
     extern __shared__ __align__(16) unsigned char ring[];
     __shared__ int s_item;
     for (;;) {
@@ -454,7 +454,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_substage32_batch(const Fused32A
         __syncthreads();
         if (t >= nitems) break;
         const int4 it = items[t];
-        if (left[it.x] <= 0) continue;  // the instance has taken its steps (uniform over the CTA)
+        // a malformed item, or an instance that has taken its steps (both uniform over the CTA)
+        if (!batch_item_ok(ctl, args, it, kTX, kTY, SW::lMag ? 8 : 5) || ctl.left[it.x] <= 0) continue;
         substage32_tile<SW>(args[it.x], it.y, it.z, it.w & 0xffff, it.w >> 16, ring);
         __syncthreads();
     }
@@ -539,9 +540,13 @@ __global__ void k_bcon_ghost32(Grid g, Consts c, Fields8f U, Fields8 Z, const do
 // BCON for a ragged batch: block b covers 128 wall cells of instance items[b].x from cell items[b].y
 template <class SW>
 __global__ void k_bcon_ghost32_batch(const Fused32Args* __restrict__ args, const int2* __restrict__ items,
-                                     const int* __restrict__ left) {
+                                     BatchCtl ctl) {
     const int2 it = items[blockIdx.x];
-    if (left[it.x] <= 0) return;
+    if (it.x < 0 || it.x >= ctl.n) {
+        if (threadIdx.x == 0 && atomicCAS(ctl.err, 0, 1) == 0) ctl.err[1] = it.x;
+        return;
+    }
+    if (ctl.left[it.x] <= 0) return;
     const Fused32Args& a = args[it.x];
     const int nPx = a.g.nx - 2, nPy = a.g.ny - 2;
     const int t = it.y + threadIdx.x;
@@ -627,9 +632,9 @@ void launch_bcon32(const Grid& g, const Consts& c, Fields8f U, Fields8 Z, const 
 }
 
 template <class SW>
-void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, const int* left, int grid,
+void batch32_launch(const Fused32Args* args, const int4* items, int nitems, int* counter, BatchCtl ctl, int grid,
                     cudaStream_t st, int* rc) {
-    k_substage32_batch<SW><<<grid, kThreads, smem_bytes<SW>(), st>>>(args, items, nitems, counter, left);
+    k_substage32_batch<SW><<<grid, kThreads, smem_bytes<SW>(), st>>>(args, items, nitems, counter, ctl);
     *rc = (int)cudaGetLastError();
 }
 
@@ -641,16 +646,16 @@ void batch32_occupancy(int* blocks, int* rc) {
 }
 
 template <class SW>
-void batch32_bcon(const Fused32Args* args, const int2* items, const int* left, int nblocks, cudaStream_t st) {
-    k_bcon_ghost32_batch<SW><<<nblocks, 128, 0, st>>>(args, items, left);
+void batch32_bcon(const Fused32Args* args, const int2* items, BatchCtl ctl, int nblocks, cudaStream_t st) {
+    k_bcon_ghost32_batch<SW><<<nblocks, 128, 0, st>>>(args, items, ctl);
 }
 
 }  // namespace
 
 int fused32_batch_substage(unsigned sw, const Fused32Args* args, const int4* items, int nitems, int* counter,
-                           const int* left, int grid, cudaStream_t st) {
+                           BatchCtl ctl, int grid, cudaStream_t st) {
     int rc = 0;
-    MHD_DISPATCH_SW(sw, batch32_launch, args, items, nitems, counter, left, grid, st, &rc);
+    MHD_DISPATCH_SW(sw, batch32_launch, args, items, nitems, counter, ctl, grid, st, &rc);
     return rc;
 }
 
@@ -660,9 +665,9 @@ int fused32_batch_occupancy(unsigned sw, int* blocks_per_sm) {
     return rc;
 }
 
-int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, const int* left, int nblocks,
+int fused32_batch_bcon(unsigned sw, const Fused32Args* args, const int2* items, BatchCtl ctl, int nblocks,
                        cudaStream_t st) {
-    MHD_DISPATCH_SW(sw, batch32_bcon, args, items, left, nblocks, st);
+    MHD_DISPATCH_SW(sw, batch32_bcon, args, items, ctl, nblocks, st);
     return (int)cudaGetLastError();
 }
 

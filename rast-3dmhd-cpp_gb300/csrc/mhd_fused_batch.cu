@@ -20,12 +20,13 @@ using BatchTile1 = Tile<32, 8>;
 using BatchTile2 = Tile<16, 8>;
 
 // item: x = instance, y = tile x, z = tile y, w = first z plane | end plane << 16.
-// left[i]: steps instance i still takes in this call (items of an instance
-// at 0 are skipped, so instances that finish early drop out of the work).
+// ctl.left[i]: steps instance i still takes in this call (items of an
+// instance at 0 are skipped, so instances that finish early drop out of the
+// work); items that fail batch_item_ok are recorded in ctl.err and skipped.
 template <class SW, class T>
 __global__ void __launch_bounds__(T::kThreads) k_substage_batch(const FusedArgs* __restrict__ args,
                                                                 const int4* __restrict__ items, int nitems,
-                                                                int* counter, const int* __restrict__ left) {
+                                                                int* counter, BatchCtl ctl) {
     extern __shared__ double ring[];
     __shared__ int s_item;
     for (;;) {
@@ -35,7 +36,8 @@ __global__ void __launch_bounds__(T::kThreads) k_substage_batch(const FusedArgs*
         __syncthreads();
         if (t >= nitems) break;
         const int4 it = items[t];
-        if (left[it.x] <= 0) continue;  // uniform over the CTA
+        // both tests are uniform over the CTA
+        if (!batch_item_ok(ctl, args, it, T::kTX, T::kTY, SW::lMag ? 8 : 5) || ctl.left[it.x] <= 0) continue;
         const FusedArgs& a = args[it.x];
         // each instance runs the variant it runs alone (isotropic or not), so
         // a batch reproduces its instances' single-instance results bit for bit
@@ -48,10 +50,13 @@ __global__ void __launch_bounds__(T::kThreads) k_substage_batch(const FusedArgs*
 // BCON for a ragged batch: block b covers 128 wall cells of instance items[b].x
 // starting at cell items[b].y.
 template <class SW>
-__global__ void k_bcon_ghost_batch(const FusedArgs* __restrict__ args, const int2* __restrict__ items,
-                                   const int* __restrict__ left) {
+__global__ void k_bcon_ghost_batch(const FusedArgs* __restrict__ args, const int2* __restrict__ items, BatchCtl ctl) {
     const int2 it = items[blockIdx.x];
-    if (left[it.x] <= 0) return;
+    if (it.x < 0 || it.x >= ctl.n) {
+        if (threadIdx.x == 0 && atomicCAS(ctl.err, 0, 1) == 0) ctl.err[1] = it.x;
+        return;
+    }
+    if (ctl.left[it.x] <= 0) return;
     const FusedArgs& a = args[it.x];
     const int nPx = a.g.nx - 2, nPy = a.g.ny - 2;
     const int t = it.y + threadIdx.x;
@@ -61,11 +66,11 @@ __global__ void k_bcon_ghost_batch(const FusedArgs* __restrict__ args, const int
 }
 
 template <class SW, class T>
-int batch_launch_t(const FusedArgs* args, const int4* items, int nitems, int* counter, const int* left, int grid,
+int batch_launch_t(const FusedArgs* args, const int4* items, int nitems, int* counter, BatchCtl ctl, int grid,
                    cudaStream_t st) {
     // the shared-memory attribute is set by batch_occupancy_t, which runs before any capture
     const size_t smem = ring_bytes<SW, T>();
-    k_substage_batch<SW, T><<<grid, T::kThreads, smem, st>>>(args, items, nitems, counter, left);
+    k_substage_batch<SW, T><<<grid, T::kThreads, smem, st>>>(args, items, nitems, counter, ctl);
     return (int)cudaGetLastError();
 }
 
@@ -77,11 +82,11 @@ int batch_occupancy_t(int* blocks) {
 }
 
 template <class SW>
-void batch_launch_sw(int tile, const FusedArgs* args, const int4* items, int nitems, int* counter, const int* left,
+void batch_launch_sw(int tile, const FusedArgs* args, const int4* items, int nitems, int* counter, BatchCtl ctl,
                      int grid, cudaStream_t st, int* rc) {
-    if (tile == 0) *rc = batch_launch_t<SW, BatchTile0>(args, items, nitems, counter, left, grid, st);
-    else if (tile == 1) *rc = batch_launch_t<SW, BatchTile1>(args, items, nitems, counter, left, grid, st);
-    else *rc = batch_launch_t<SW, BatchTile2>(args, items, nitems, counter, left, grid, st);
+    if (tile == 0) *rc = batch_launch_t<SW, BatchTile0>(args, items, nitems, counter, ctl, grid, st);
+    else if (tile == 1) *rc = batch_launch_t<SW, BatchTile1>(args, items, nitems, counter, ctl, grid, st);
+    else *rc = batch_launch_t<SW, BatchTile2>(args, items, nitems, counter, ctl, grid, st);
 }
 
 template <class SW>
@@ -92,8 +97,8 @@ void batch_occupancy_sw(int tile, int* blocks, int* rc) {
 }
 
 template <class SW>
-void batch_bcon_sw(const FusedArgs* args, const int2* items, const int* left, int nblocks, cudaStream_t st) {
-    k_bcon_ghost_batch<SW><<<nblocks, 128, 0, st>>>(args, items, left);
+void batch_bcon_sw(const FusedArgs* args, const int2* items, BatchCtl ctl, int nblocks, cudaStream_t st) {
+    k_bcon_ghost_batch<SW><<<nblocks, 128, 0, st>>>(args, items, ctl);
 }
 
 // end of a batched step: one step fewer left for every instance still stepping
@@ -111,9 +116,9 @@ __global__ void k_batch_tick(int* left, int n) {
 #endif
 
 int MHD_BATCH_FN(fused_batch_substage)(unsigned sw, int tile, const FusedArgs* args, const int4* items, int nitems,
-                                       int* counter, const int* left, int grid, cudaStream_t st) {
+                                       int* counter, BatchCtl ctl, int grid, cudaStream_t st) {
     int rc = 0;
-    MHD_DISPATCH_SW(sw, batch_launch_sw, tile, args, items, nitems, counter, left, grid, st, &rc);
+    MHD_DISPATCH_SW(sw, batch_launch_sw, tile, args, items, nitems, counter, ctl, grid, st, &rc);
     return rc;
 }
 
@@ -125,9 +130,9 @@ int MHD_BATCH_FN(fused_batch_occupancy)(unsigned sw, int tile, int* blocks_per_s
 
 #if MHD_BATCH_UXY
 // the wall kernel does not depend on the grid kind: built once
-int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, const int* left, int nblocks,
+int fused_batch_bcon(unsigned sw, const FusedArgs* args, const int2* items, BatchCtl ctl, int nblocks,
                      cudaStream_t st) {
-    MHD_DISPATCH_SW(sw, batch_bcon_sw, args, items, left, nblocks, st);
+    MHD_DISPATCH_SW(sw, batch_bcon_sw, args, items, ctl, nblocks, st);
     return (int)cudaGetLastError();
 }
 
