@@ -77,3 +77,26 @@ def test_autotuner_scratch_counts_against_the_budget():
         r.arrival = 0.0
     st2 = Server(3 * need, quantum=4, target_cells=1).run(roomy, realtime=False)
     assert st2["tune_skipped"] == 0 and st2["zrange"]["fp64"] in (64, 32, 16)
+
+
+def test_realtime_mixed_stream_with_tuning_overlaps_and_matches_alone():
+    """Both precisions' batches running at once while requests are admitted,
+    both autotuned (tile shape and z range), step limits and balanced quanta
+    on: every request completes, no work item fails its check, and the
+    results of a few requests equal the same requests served alone."""
+    reqs = poisson_requests(24, rate=200.0, seed=17, grid_min=(32, 32, 32), grid_max=(64, 64, 64),
+                            steps=(10, 40), fp32_fraction=0.5)
+    cells = sum(r.case.cells for r in reqs)
+    srv = Server(64 << 30, quantum=6, keep_results=True, target_cells=cells // 3)
+    st = srv.run(reqs, realtime=True)
+    assert st["requests"] == len(reqs) and srv.completed == len(reqs)
+    assert st["max_resident"] >= 4
+    assert st["zrange"]["fp64"] is not None and st["zrange"]["fp32"] is not None
+    for r in reqs[:4]:
+        alone = Request(rid=r.rid, case=r.case, steps=r.steps, precision=r.precision, arrival=0.0)
+        s1 = Server(8 << 30, quantum=6, tile=st["tile"], keep_results=True)
+        s1.zrange = dict(st["zrange"])           # the same tuned work-item shapes as in the mix
+        s1.tuned = {"fp64": True, "fp32": True}
+        s1.run([alone], realtime=False)
+        for k in STATE_FIELDS[:r.case.nfields]:
+            assert np.array_equal(r.result[k], alone.result[k]), (r.rid, r.precision, k)
