@@ -239,7 +239,8 @@ struct Fused32Args {
     double* FT;    // FP64 persistent temperature right-hand side (lShr only)
     const double *bgR, *bgT;     // reference profiles rho0(z), T0(z)
     const double *dzT0, *d2zT0;  // their premultiplied first and second z derivatives
-    const float* zf;             // [7][nz] float cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA
+    const float* zf;             // [8][nz] float cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA, and the
+                                 // profiles' hydrostatic residual rho0 GRAV - D_z(rho0 T0)
     double gdt, zdt;
     double timt;
     int substage;

@@ -5,13 +5,17 @@
 // mean of the uploaded state), so the large hydrostatic part of rho and T
 // never passes through FP32; the other six fields have a zero profile.
 // Arithmetic:
-//   FP64: the reconstruction rho = rho0 + drho, T = T0 + dT, the equation of
-//         state p = rho T, the pressure gradient and gravity (the terms that
-//         cancel in hydrostatic balance), and the RK3 register
+//   FP64: the reconstruction rho = rho0 + drho, T = T0 + dT and the equation
+//         of state p = rho T at every point, kept as its deviation
+//         dp = p - rho0 T0 from the plane's profile value; the hydrostatic
+//         residual of the profiles, rho0 GRAV - D_z(rho0 T0), per z on the
+//         host (its two terms nearly cancel); and the RK3 register
 //         Z (U' = Z + gamma dt F, Z' = U' + zeta dt F, 3dmhdsub.h:168-192);
-//   FP32: every other stencil of fluxes() (advection, conduction, viscous
-//         terms and heating, Coriolis, induction, Lorentz force, Ohmic
-//         heating; 3dmhdsub.h:204-695).
+//   FP32: every stencil of fluxes() (3dmhdsub.h:204-695), the pressure
+//         gradient and gravity among them as stencils of the deviations
+//         (-D_x dp, -D_y dp, drho GRAV - D_z dp, added to the residual): the
+//         large parts that cancel in hydrostatic balance never pass through
+//         FP32.
 // The FP64 register Z also carries the state from one step to the next (the
 // last substage writes U' into it, BCON keeps its wall values), so FP32
 // rounding enters only through the stencil inputs, never into the state.
@@ -33,7 +37,8 @@ constexpr int kPY = kTY + 2;
 constexpr int kPlane = kPX * kPY;
 
 // FP32 quantities per plane point; the pressure is kept in FP64 beside them
-enum QF { F_RU = 0, F_RV, F_RW, F_DT, F_DRO, F_RI, F_U, F_V, F_W, F_BX, F_BY, F_BZ, F_NQ };
+// F_DP: the pressure deviation p - rho0 T0 of the point (p = rho T in FP64)
+enum QF { F_RU = 0, F_RV, F_RW, F_DT, F_DRO, F_RI, F_U, F_V, F_W, F_DP, F_BX, F_BY, F_BZ, F_NQ };
 
 template <class SW>
 constexpr int nqf() {
@@ -42,18 +47,16 @@ constexpr int nqf() {
 
 template <class SW>
 constexpr size_t plane_bytes() {
-    return (size_t)nqf<SW>() * kPlane * sizeof(float) + (size_t)kPlane * sizeof(double);
+    return (size_t)nqf<SW>() * kPlane * sizeof(float);
 }
 
 struct RingPtrs {
     float* f;
-    double* p;
 };
 
 template <class SW>
 __device__ __forceinline__ RingPtrs ring_slot(unsigned char* ring, int slot) {
-    unsigned char* b = ring + (size_t)slot * plane_bytes<SW>();
-    return {reinterpret_cast<float*>(b + (size_t)kPlane * sizeof(double)), reinterpret_cast<double*>(b)};
+    return {reinterpret_cast<float*>(ring + (size_t)slot * plane_bytes<SW>())};
 }
 
 // Raw FP32 fields of one plane (8 with lMag, else 5), staged in shared
@@ -74,14 +77,17 @@ __device__ __forceinline__ float* raw_stage(unsigned char* ring) {
 }
 
 // The derived quantities of one plane point from its raw fields (get(f) is
-// field f of the point): 1/rho and the velocities in FP32, p = rho T in FP64.
+// field f of the point): 1/rho and the velocities in FP32; the equation of
+// state p = rho T in FP64, stored as its deviation from the plane's
+// rho0 T0 (p0), which the x/y differences of the pressure do not see and
+// whose z differences enter through the per-z hydrostatic residual.
 template <class SW, class Get>
-__device__ __forceinline__ void put_point(RingPtrs r, int k, double r0, double t0, Get get) {
+__device__ __forceinline__ void put_point(RingPtrs r, int k, double r0, double t0, double p0, Get get) {
     const float ru = get(S_RU), rv = get(S_RV), rw = get(S_RW);
     const float dt = get(S_TT), dro = get(S_RO);
     const double ro = r0 + widen_f32(dro), tt = t0 + widen_f32(dt);
     const float ri = 1.0f / narrow_f64(ro);
-    r.p[k] = ro * tt;
+    r.f[F_DP * kPlane + k] = narrow_f64(fma(ro, tt, -p0));
     r.f[F_RU * kPlane + k] = ru;
     r.f[F_RV * kPlane + k] = rv;
     r.f[F_RW * kPlane + k] = rw;
@@ -105,13 +111,13 @@ __device__ __forceinline__ void load_plane32(const Fused32Args& a, unsigned char
                                              int y0) {
     RingPtrs r = ring_slot<SW>(ring, slot);
     const Grid& g = a.g;
-    const double r0 = a.bgR[z], t0 = a.bgT[z];
+    const double r0 = a.bgR[z], t0 = a.bgT[z], p0 = r0 * t0;
     for (int k = threadIdx.x; k < kPlane; k += kThreads) {
         const int hx = k % kPX, hy = k / kPX;
         const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
         if (gx >= g.nx || gy >= g.ny) continue;
         const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
-        put_point<SW>(r, k, r0, t0, [&](int f) { return a.U.p[f][i]; });
+        put_point<SW>(r, k, r0, t0, p0, [&](int f) { return a.U.p[f][i]; });
     }
 }
 
@@ -145,11 +151,11 @@ __device__ __forceinline__ void derive_plane32(const Fused32Args& a, unsigned ch
     const float* raw = raw_stage<SW>(ring);
     RingPtrs r = ring_slot<SW>(ring, slot);
     const Grid& g = a.g;
-    const double r0 = a.bgR[z], t0 = a.bgT[z];
+    const double r0 = a.bgR[z], t0 = a.bgT[z], p0 = r0 * t0;
     for (int k = threadIdx.x; k < kPlane; k += kThreads) {
         const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
         if (gx >= g.nx || gy >= g.ny) continue;
-        put_point<SW>(r, k, r0, t0, [&](int f) { return raw[f * kPlane + k]; });
+        put_point<SW>(r, k, r0, t0, p0, [&](int f) { return raw[f * kPlane + k]; });
     }
 }
 
@@ -190,13 +196,13 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
     float ohm = (float)(c.OBETA * c.ORM * c.OCV);
     float tmpc = (float)(c.OCV / c.REPR);
     float obeta = (float)c.OBETA, orm = (float)c.ORM, c43 = (float)c.C43;
-    float omz = (float)c.OMZ, omx = (float)c.OMX;
+    float omz = (float)c.OMZ, omx = (float)c.OMX, grav = (float)c.GRAV;
     // GB300 runs float<->double conversions on its FP64 pipe; under the 80-register
     // cap the compiler would recompute these converted constants inside the z loop
     // (12 conversions per cell, measured).  Opaque copies stay in registers instead.
     asm volatile("" : "+f"(omz), "+f"(omx), "+f"(cx1), "+f"(cx2a), "+f"(cx2b), "+f"(cy1), "+f"(cy2a), "+f"(cy2b));
     asm volatile("" : "+f"(c13ore), "+f"(kxy), "+f"(ore), "+f"(ore43), "+f"(ocvore), "+f"(ocv), "+f"(ohm), "+f"(tmpc));
-    asm volatile("" : "+f"(obeta), "+f"(orm), "+f"(c43));
+    asm volatile("" : "+f"(obeta), "+f"(orm), "+f"(c43), "+f"(grav));
     // RK coefficients: from the host, or from the device time-step record; a
     // halted record (dt below 1e-8) turns the substage into a copy of the state
     const double gdt = a.dtp ? a.gam * a.dtp[0] : a.gdt;
@@ -226,7 +232,6 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             auto YM = [&](int q) { return P0[q * kPlane + pc - kPX]; };
             auto ZP = [&](int q) { return Pp[q * kPlane + pc]; };
             auto ZM = [&](int q) { return Pm[q * kPlane + pc]; };
-            const double cz1d = a.k.cz1[z];
             const int nzz = g.nz;
             const float cz1 = a.zf[z], cz2a = a.zf[nzz + z], cz2b = a.zf[2 * nzz + z];
             auto Dx = [&](int q) { return (XP(q) - XM(q)) * cx1; };
@@ -254,16 +259,17 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 for (int f = 0; f < nfp; f++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Z.p[f] + inx));
                 if constexpr (SW::lShr) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.FT + inx));
             }
-            const double ro = a.bgR[z] + widen_f32(C0(F_DRO));
-            const double tt = a.bgT[z] + widen_f32(C0(F_DT));
-            const float ri = C0(F_RI), ttf = narrow_f64(tt);
+            const float ri = C0(F_RI), ttf = narrow_f64(a.bgT[z]) + C0(F_DT);
             const float u = C0(F_U), v = C0(F_V), w = C0(F_W);
 
-            // ---- FP64: pressure gradient and gravity (3dmhdsub.h:266-272)
-            const double pxp = R0.p[pc + 1], pxm = R0.p[pc - 1], pyp = R0.p[pc + kPX], pym = R0.p[pc - kPX];
-            const double fu64 = -(pxp - pxm) * cx1d;
-            const double fv64 = -(pyp - pym) * cy1d;
-            const double fw64 = fma(ro, c.GRAV, -(Rp.p[pc] - Rm.p[pc]) * cz1d);
+            // ---- pressure gradient and gravity (3dmhdsub.h:266-272).  p = p0(z) + dp
+            // with p0 = rho0 T0 constant over the plane: x and y see only dp; in z the
+            // large, cancelling part rho0 GRAV - D_z p0 is the hydrostatic residual of
+            // the profiles, computed per z in FP64 on the host (zf row 7), and the
+            // deviations drho GRAV - D_z dp are stenciled here.
+            float fu = -(XP(F_DP) - XM(F_DP)) * cx1;
+            float fv = -(YP(F_DP) - YM(F_DP)) * cy1;
+            float fw = fmaf(C0(F_DRO), grav, fmaf(-(ZP(F_DP) - ZM(F_DP)), cz1, a.zf[7 * nzz + z]));
 
             // ---- continuity (3dmhdsub.h:204-227)
             float rwz = Dz(F_RW);
@@ -272,7 +278,6 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             const float fr = -(Dx(F_RU) + Dy(F_RV) + rwz);
 
             // ---- momentum advection
-            float fu = 0.f, fv = 0.f, fw = 0.f;
             fu -= fmaf(XP(F_RU), XP(F_U), -XM(F_RU) * XM(F_U)) * cx1;
             fu -= fmaf(YP(F_RU), YP(F_V), -YM(F_RU) * YM(F_V)) * cy1;
             fu -= fmaf(ZP(F_RU), ZP(F_W), -ZM(F_RU) * ZM(F_W)) * cz1;
@@ -398,7 +403,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             // ---- FP64 RK3 register (3dmhdsub.h:168-192)
             double ftd = widen_f32(ft);
             if constexpr (SW::lShr) ftd += a.FT[i];
-            const double fl[8] = {fu64 + widen_f32(fu), fv64 + widen_f32(fv), fw64 + widen_f32(fw), ftd,
+            const double fl[8] = {widen_f32(fu), widen_f32(fv), widen_f32(fw), ftd,
                                   widen_f32(fr), widen_f32(w1), widen_f32(w2), widen_f32(w3)};
             const int nf = SW::lMag ? 8 : 5;
             const double r0z = a.bgR[z], t0z = a.bgT[z];
