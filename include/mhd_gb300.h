@@ -291,13 +291,25 @@ typedef struct mhd_static_params {
  * `state` receives nf x nz x ny x nx doubles, field-major as in
  * mhd_upload_state, bit-identical to the reference run with the same
  * parameters and rank grid.  Uses THETA, GRAV, BETA, the switches and the
- * grid of `p` only; needs no context and no GPU.  With lMag and AMPB = 0 the
- * field is that of tube() with nTube = 0 (zero).  MHD_ERR_UNSUPPORTED with
- * MHD_SW_LREM (that background is a tabulated stellar model) and for
+ * grid of `p` only (with MHD_SW_LREM also RE and PR); needs no context and
+ * no GPU.  With lMag and AMPB = 0 the field is that of tube() with nTube = 0
+ * (zero).  With MHD_SW_LREM the background comes from the ODE of
+ * getbackground (3dmhdphsic.h:357-362, integrated by ODEINT/RKQC/RK4,
+ * 3dmhdphsic.h:409-522) instead of the PZP/SIGMA/POLYS model; MHD_ERR_NUMERIC
+ * where the reference aborts there (a level at depth exactly 2, e.g. with
+ * zMax = 2: "Stepsize not significant in RKQC").  MHD_ERR_UNSUPPORTED for
  * nTube 1-5, which give the reference no state: 1 and 3 abort in qromb
  * ("Failure in polint", 3dmhdphsic.h:207-208), 2, 4 and 5 do not compile
  * (3dmhdphsic.h:843-844, 951-954, 984). */
 int mhd_static_state(const mhd_params* p, const mhd_static_params* s, double* state);
+/* The rest of Static()'s lRem set-up (3dmhdphsic.h:565-594, 616-681): the
+ * radiative conductivity of every global z plane, rkapa[nz] (RKAPA), its z
+ * derivative dkapa[nz] (DKAPA), the wall ghosts repeating the walls, and
+ * walls[3] = {TU, DZTU, DZTB}, which the run then passes in mhd_params and as
+ * the RKAPA / DKAPA metric arrays.  Bit-identical with the compiled reference;
+ * MHD_ERR_NUMERIC where it aborts (as mhd_static_state). */
+int mhd_static_lrem_profile(const mhd_params* p, const mhd_static_params* s, double* rkapa, double* dkapa,
+                            double* walls);
 
 /* Self-check: the integer-pipe float<->double conversions the FP32-storage
  * kernels use against the hardware conversions, on n test patterns of seed;

@@ -248,6 +248,17 @@ int main(int argc, char** argv) {
         /* a fresh start: Static() then communicate(), as main() (3dmhd.cpp:111-142) */
         Static();
         communicate();
+#if lRem
+        /* Static() also derived the conductivity profile of every plane and the wall
+         * values (3dmhdphsic.h:565-594): RKAPA / DKAPA go out in the FU / FV slots,
+         * TU / DZTU / DZTB in the trailer */
+        for (int z = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    FU[z][y][x] = RKAPA[z];
+                    FV[z][y][x] = DKAPA[z];
+                }
+#endif
     } else if (h.mode == 3) {
         step_block_ZETA0(FORRANGE);
         fluxes(FORRANGE);
@@ -272,6 +283,11 @@ int main(int argc, char** argv) {
         trailer[2] = secs;
         trailer[3] = (double)nPE;
         trailer[4] = DT;
+#if lRem
+        trailer[5] = TU;
+        trailer[6] = DZTU;
+        trailer[7] = DZTB;
+#endif
         for (int n = 0; n < nsteps && n < (int)dt_hist.size(); n++) trailer[16 + n] = dt_hist[n];
         off_t off = (off_t)(sizeof(double) * 24 * nglob);
         if (pwrite(fd, trailer.data(), sizeof(double) * trailer.size(), off) != (ssize_t)(sizeof(double) * trailer.size()))

@@ -220,6 +220,8 @@ def read_output(path: Path, case: Case, nsteps: int) -> dict:
     out["seconds"] = float(tr[2])
     out["DT"] = float(tr[4])
     out["dt_hist"] = tr[16:16 + nsteps].copy()
+    # mode "static" with lRem: the wall values Static() derived
+    out["TU"], out["DZTU"], out["DZTB"] = float(tr[5]), float(tr[6]), float(tr[7])
     return out
 
 

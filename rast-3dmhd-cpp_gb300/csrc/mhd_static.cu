@@ -2,7 +2,9 @@
 // (3dmhdphsic.h:549-763) followed by communicate(), computed on the host for a
 // caller that starts runs without the reference's driver.  No device work.
 //
-// Static() builds the hydrostatic background by integrating
+// Static() builds the hydrostatic background (with lRem: the ODE background
+// of getbackground below, which also gives the conductivity profile and the
+// wall values, mhd_static_lrem_profile) by integrating
 //   dY0/dzz = THETA / kappa(zz) / dzzdz,  dY1/dzz = GRAV / (1 + Y0) / dzzdz
 // (derivs, 3dmhdphsic.h:347-355) over the computational coordinate, one
 // Bulirsch-Stoer step per grid interval (bsstep / mmid / rzextr,
@@ -127,6 +129,125 @@ double bs_step(const StaticModel& m, double* y, const double* dydx, double& x, d
     }
 }
 
+// ---- lRem: the background of getbackground (3dmhdphsic.h:357-362) --------
+// An ODE in the physical depth x for (T, P): dT/dx = min(0.4 / kappa, 0.41)
+// (radiative gradient capped at the adiabatic one), dP/dx = P / T, with the
+// conductivity kappa = rho + (1.25 - rho) exp(-5 x) (kappa and derivs1,
+// 3dmhdphsic.h:389-405), integrated from x = 2 (T = P = 1) to each level by
+// classical RK4 steps under step doubling with error control (RK4, RKQC and
+// ODEINT, 3dmhdphsic.h:409-522, the published Numerical Recipes scheme).
+double lrem_kappa(double z, double rho) { return rho + (1.25f - rho) * std::exp(-5.0f * z); }
+
+void lrem_slope(double x, const double* y, double* d) {
+    const double nad = 0.41f, os = 1.0f;
+    const double nrad = 0.4f / lrem_kappa(x, y[1] / y[0]);
+    d[0] = (nrad <= os * nad) ? nrad : nad;
+    d[1] = y[1] / y[0];
+}
+
+void lrem_rk4(const double* y, const double* dydx, double x, double h, double* yout) {
+    double yt[2], dyt[2], dym[2];
+    const double hh = h * 0.5f, h6 = h / 6.0f, xh = x + hh;
+    for (int i = 0; i < 2; i++) yt[i] = y[i] + hh * dydx[i];
+    lrem_slope(xh, yt, dyt);
+    for (int i = 0; i < 2; i++) yt[i] = y[i] + hh * dyt[i];
+    lrem_slope(xh, yt, dym);
+    for (int i = 0; i < 2; i++) {
+        yt[i] = y[i] + h * dym[i];
+        dym[i] = dyt[i] + dym[i];
+    }
+    lrem_slope(x + h, yt, dyt);
+    for (int i = 0; i < 2; i++) yout[i] = y[i] + h6 * (dydx[i] + dyt[i] + 2.0f * dym[i]);
+}
+
+// One controlled step (two half steps against one full step); false where
+// the reference aborts ("Stepsize not significant in RKQC").
+bool lrem_controlled_step(double* y, double* dydx, double& x, double htry, double eps, const double* yscal,
+                          double& hdid, double& hnext) {
+    const double fcor = 1.0f / 15.0f, safety = 0.9f, errcon = 6.0e-4f, pgrow = -0.20f, pshrnk = -0.25f;
+    const double xsav = x;
+    const double ysav[2] = {y[0], y[1]}, dysav[2] = {dydx[0], dydx[1]};
+    double ytemp[2];
+    double h = htry;
+    for (;;) {
+        const double hh = 0.5f * h;
+        lrem_rk4(ysav, dysav, xsav, hh, ytemp);
+        x = xsav + hh;
+        lrem_slope(x, ytemp, dydx);
+        lrem_rk4(ytemp, dydx, x, hh, y);
+        x = xsav + h;
+        if (x == xsav) return false;
+        lrem_rk4(ysav, dysav, xsav, h, ytemp);
+        double errmax = 0.0f;
+        for (int i = 0; i < 2; i++) {
+            ytemp[i] = y[i] - ytemp[i];
+            errmax = std::max(errmax, std::fabs(ytemp[i] / yscal[i]));
+        }
+        errmax = errmax / eps;
+        if (errmax > 1.0) {
+            h = safety * h * std::pow(errmax, pshrnk);
+        } else {
+            hdid = h;
+            hnext = errmax > errcon ? safety * h * std::pow(errmax, pgrow) : 4.0f * h;
+            break;
+        }
+    }
+    for (int i = 0; i < 2; i++) y[i] += ytemp[i] * fcor;
+    return true;
+}
+
+// T and rho at depth x; false where the reference aborts.
+bool lrem_background(double x, double& t, double& rho) {
+    const double tiny = 1.0e-30f, h1 = 1e-4, hmin = 1e-50, eps = 1e-8;
+    const double x1 = 2.0f, x2 = x;
+    double y[2] = {1.0, 1.0}, dydx[2], yscal[2];
+    double xc = x1, h = (x2 > x1) ? h1 : -h1;
+    for (int nstp = 1; nstp <= 1000; nstp++) {
+        lrem_slope(xc, y, dydx);
+        for (int i = 0; i < 2; i++) yscal[i] = std::abs(y[i]) + std::abs(h * dydx[i]) + tiny;
+        if ((xc + h - x2) * (xc + h - x1) > 0) h = x2 - xc;
+        double hdid, hnext;
+        if (!lrem_controlled_step(y, dydx, xc, h, eps, yscal, hdid, hnext)) return false;
+        if ((xc - x2) * (x2 - x1) >= 0) {
+            t = y[0];
+            rho = y[1] / y[0];
+            return true;
+        }
+        if (std::abs(hnext) < hmin) return false;
+        h = hnext;
+    }
+    return false;  // "Too many steps."
+}
+
+// The lRem part of Static() (3dmhdphsic.h:565-594): T, rho and the scaled
+// conductivity RK with its z derivative DRK on the nPz levels, and the wall
+// values TU, DZTU, DZTB.  False where the reference aborts.
+bool lrem_profile(const mhd_params* p, double zMax, std::vector<double>& T, std::vector<double>& R,
+                  std::vector<double>& RK, std::vector<double>& DRK, double walls[3]) {
+    const int nPz = p->nPz;
+    mhd_constants k;
+    mhd_compute_constants(p, &k);
+    T.assign(nPz, 0.0);
+    R.assign(nPz, 0.0);
+    RK.assign(nPz, 0.0);
+    DRK.assign(nPz, 0.0);
+    for (int j = 0; j < nPz; j++) {
+        const double code = static_cast<float>(j) / static_cast<float>(nPz - 1);
+        const double sz = code * zMax;  // mkGrid with a uniform grid
+        if (!lrem_background(sz, T[j], R[j])) return false;
+        RK[j] = lrem_kappa(sz, R[j]);
+        RK[j] *= 8.07f * p->THETA * k.REPR;
+    }
+    const double sdzzdz = 1.0f / zMax;
+    DRK[0] = (-3.0f * RK[0] + 4.0f * RK[1] - RK[2]) * k.hz * sdzzdz;
+    for (int j = 1; j < nPz - 1; j++) DRK[j] = (RK[j + 1] - RK[j - 1]) * k.hz * sdzzdz;
+    DRK[nPz - 1] = (3.0f * RK[nPz - 1] - 4.0f * RK[nPz - 2] + RK[nPz - 3]) * k.hz * sdzzdz;
+    walls[0] = T[0];
+    walls[1] = T[0] - 4.0f / 3.0f * T[1] + 1.0f / 3.0f * T[2];
+    walls[2] = T[nPz - 1] - 4.0f / 3.0f * T[nPz - 2] + 1.0f / 3.0f * T[nPz - 3];
+    return true;
+}
+
 // RAN2 (3dmhdphsic.h:523-547): a shuffled linear congruential generator
 struct Ran2 {
     static constexpr int M = 714025, IA = 1366, IC = 150889;
@@ -157,7 +278,8 @@ struct Ran2 {
 
 extern "C" int mhd_static_state(const mhd_params* p, const mhd_static_params* s, double* state) {
     if (!p || !s || !state || !s->ZEE) return MHD_ERR_INVALID;
-    if (p->switches & MHD_SW_LREM) return MHD_ERR_UNSUPPORTED;  // lRem's background is a stellar model
+    const bool rem = (p->switches & MHD_SW_LREM) != 0;
+    if (rem && (p->switches & MHD_SW_LSHR)) return MHD_ERR_UNSUPPORTED;
     if (s->nTube < 0 || s->nTube > 5) return MHD_ERR_INVALID;
     // tube models 1-5 leave the reference without a state (abort or no build)
     if (s->nTube != 0 && (p->switches & MHD_SW_LMAG) && s->AMPB == 0.0) return MHD_ERR_UNSUPPORTED;
@@ -171,7 +293,11 @@ extern "C" int mhd_static_state(const mhd_params* p, const mhd_static_params* s,
 
     // background profile T[k], R[k] on the nPz interior levels
     std::vector<double> T(nPz, 1.0), R(nPz, 1.0);
-    if (!shr) {
+    if (rem) {
+        std::vector<double> RK, DRK;
+        double walls[3];
+        if (!lrem_profile(p, s->zMax, T, R, RK, DRK, walls)) return MHD_ERR_NUMERIC;
+    } else if (!shr) {
         StaticModel m{p->THETA, p->GRAV, s->zMax, s->PZP, s->SIGMA,
                       p->GRAV == 0.0 ? 1.0f : (s->POLYS + 1.0f) * p->THETA / p->GRAV};
         const double eps = 1.0E-12f, dzz = 1.0f / float(nPz - 1);
@@ -238,5 +364,23 @@ extern "C" int mhd_static_state(const mhd_params* p, const mhd_static_params* s,
                 F(f, z, y, nx - 1) = F(f, z, y, 1);
             }
         }
+    return MHD_OK;
+}
+
+extern "C" int mhd_static_lrem_profile(const mhd_params* p, const mhd_static_params* s, double* rkapa, double* dkapa,
+                                       double* walls) {
+    if (!p || !s || !rkapa || !dkapa || !walls) return MHD_ERR_INVALID;
+    if (!(p->switches & MHD_SW_LREM) || (p->switches & MHD_SW_LSHR)) return MHD_ERR_INVALID;
+    if (p->nPz < 4) return MHD_ERR_INVALID;
+    std::vector<double> T, R, RK, DRK;
+    if (!lrem_profile(p, s->zMax, T, R, RK, DRK, walls)) return MHD_ERR_NUMERIC;
+    // global plane gz takes level gz - 1; the wall ghosts repeat the walls
+    // (RKAPA = RK, DKAPA = DRK of Static()'s plane assignment, 3dmhdphsic.h:616-681)
+    const int nz = p->nPz + 2;
+    for (int z = 0; z < nz; z++) {
+        const int j = std::min(std::max(z - 1, 0), p->nPz - 1);
+        rkapa[z] = RK[j];
+        dkapa[z] = DRK[j];
+    }
     return MHD_OK;
 }

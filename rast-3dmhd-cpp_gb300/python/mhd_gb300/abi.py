@@ -119,6 +119,7 @@ SIGNATURES = {
     "mhd_set_plume": [C.c_void_p, C.POINTER(MhdPlume)],
     "mhd_selftest_convert": [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "mhd_static_state": [C.POINTER(MhdParams), C.POINTER(MhdStaticParams), _DP],
+    "mhd_static_lrem_profile": [C.POINTER(MhdParams), C.POINTER(MhdStaticParams), _DP, _DP, _DP],
     "mhd_diagnostics": [C.c_void_p, C.POINTER(MhdDiag)],
     "mhd_sync": [C.c_void_p],
     "mhd_batch_create": [C.POINTER(C.c_void_p), _DP, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)],

@@ -351,8 +351,8 @@ def lrem_cases() -> dict[str, Case]:
 def static_cases() -> dict[str, Case]:
     """Fresh-start cases of Static(): the polytrope with a Bx layer and noise
     on 2 x 2 ranks, the conductivity step (PZP, SIGMA, POLYS) on 1 x 4 ranks
-    with a layer that meets the z-rank edges, and lShr's RV noise with the
-    zero field of tube() (nTube = 0)."""
+    with a layer that meets the z-rank edges, lShr's RV noise with the
+    zero field of tube() (nTube = 0), and lRem's ODE background."""
     base = dict(nPx=12, nPy=8, nPz=8, seed=7)
     return {
         "static_layer": Case(name="static_layer", nPEy=2, nPEz=2, AMPT=0.02, AMPB=0.1, BFH=0.5, BZP=1.2, **base),
@@ -361,6 +361,10 @@ def static_cases() -> dict[str, Case]:
         "static_shr": Case(name="static_shr", lShr=True, lRot=True, nPEy=2, nPEz=2, AMPT=0.03, **base),
         "static_hydro": Case(name="static_hydro", lMag=False, nPEy=4, nPEz=2, PZP=0.3, SIGMA=0.05, POLYS=1.0,
                              AMPT=0.01, **base),
+        # lRem: the ODE background of getbackground (zMax = 1.5: no level at
+        # depth 2, where the reference's integration aborts)
+        "static_lrem": Case(name="static_lrem", lMag=True, lRem=True, zMax=1.5, nPEy=2, nPEz=2, AMPT=0.02,
+                            AMPB=0.1, BFH=0.5, BZP=0.9, **base),
     }
 
 

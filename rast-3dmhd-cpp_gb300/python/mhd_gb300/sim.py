@@ -62,6 +62,19 @@ def static_state(case: Case, nPEy: int | None = None, nPEz: int | None = None) -
     return {k: out[i] for i, k in enumerate(STATE_FIELDS[:case.nfields])}
 
 
+def static_lrem_profile(case: Case) -> dict:
+    """With lRem, the conductivity profile and wall values Static() derives
+    with its background (3dmhdphsic.h:565-594): RKAPA and DKAPA of every z
+    plane (ghosts included) and TU, DZTU, DZTB (mhd_static_lrem_profile)."""
+    L = abi.load()
+    p, keep = params_for(case)
+    sp = abi.MhdStaticParams()
+    sp.zMax = float(case.zMax)
+    rk, drk, walls = np.empty(case.nz), np.empty(case.nz), np.empty(3)
+    abi.check(L.mhd_static_lrem_profile(C.byref(p), C.byref(sp), _dp(rk), _dp(drk), _dp(walls)))
+    return {"RKAPA": rk, "DKAPA": drk, "TU": float(walls[0]), "DZTU": float(walls[1]), "DZTB": float(walls[2])}
+
+
 class Simulation:
     """One device-resident 3dmhd instance."""
 

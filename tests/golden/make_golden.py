@@ -61,6 +61,10 @@ def static_fixtures() -> None:
         out = {"ZEE": coordinates(case)[2]}
         for k in STATE_FIELDS[:case.nfields]:
             out["static_" + k] = r[k]
+        if case.lRem:  # the harness returns RKAPA / DKAPA in the FU / FV slots
+            out["static_RKAPA"] = r["FU"][:, 1, 1].copy()
+            out["static_DKAPA"] = r["FV"][:, 1, 1].copy()
+            out["static_walls"] = np.array([r["TU"], r["DZTU"], r["DZTB"]])
         np.savez_compressed(HERE / f"{name}.npz", **out)
         manifest[name] = case.to_dict()
         print("wrote", name)

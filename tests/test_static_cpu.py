@@ -87,7 +87,7 @@ def test_static_rejects_what_is_not_built():
     sp = abi.MhdStaticParams(nPEy=2, nPEz=2, zMax=case.zMax)
     sp.ZEE = zee.ctypes.data_as(C.POINTER(C.c_double))
     dp = out.ctypes.data_as(C.POINTER(C.c_double))
-    p, _keep = params_for(case.replace(lRem=True))
+    p, _keep = params_for(case.replace(lRem=True, lShr=True))  # lRem with lShr has no reference behaviour
     assert L.mhd_static_state(C.byref(p), C.byref(sp), dp) == abi.MHD_ERR_UNSUPPORTED
     p, _keep = params_for(case)
     sp.nPEz = 3  # nPz = 8 does not split over 3 z ranks
@@ -126,3 +126,44 @@ def test_static_live_reference_other_rank_grid():
     got = static_state(case)
     for k in STATE_FIELDS[:case.nfields]:
         assert np.array_equal(r[k], got[k]), k
+
+
+def test_static_lrem_profile_matches_reference_fixture():
+    """lRem's background (getbackground: RK4 steps under step doubling from
+    depth 2, 3dmhdphsic.h:357-522) also gives RKAPA / DKAPA of every plane
+    and the wall values TU, DZTU, DZTB (3dmhdphsic.h:565-594): bit-identical
+    with the compiled reference."""
+    from mhd_gb300.sim import static_lrem_profile
+    case = _case("static_lrem")
+    ref = np.load(GOLDEN / "static_lrem.npz")
+    got = static_lrem_profile(case)
+    assert np.array_equal(got["RKAPA"], ref["static_RKAPA"])
+    assert np.array_equal(got["DKAPA"], ref["static_DKAPA"])
+    assert [got["TU"], got["DZTU"], got["DZTB"]] == ref["static_walls"].tolist()
+    assert np.all(np.diff(got["RKAPA"][1:-1]) != 0.0)
+
+
+def test_static_lrem_aborts_where_the_reference_does():
+    """With zMax = 2 the last level lies at depth 2, where the integration
+    starts: the reference's first step is clipped to zero and it aborts
+    ("Stepsize not significant in RKQC", 3dmhdphsic.h:480-483); the library
+    returns MHD_ERR_NUMERIC for the state and the profile."""
+    import ctypes as C
+    from mhd_gb300.sim import params_for
+    case = _case("static_lrem").replace(zMax=2.0, name="static_lrem_z2")
+    L = abi.load()
+    p, _keep = params_for(case)
+    sp = abi.MhdStaticParams(nPEy=2, nPEz=2, zMax=2.0)
+    zee = np.ascontiguousarray(coordinates(case)[2])
+    sp.ZEE = zee.ctypes.data_as(C.POINTER(C.c_double))
+    out = np.empty((case.nfields,) + case.shape)
+    assert L.mhd_static_state(C.byref(p), C.byref(sp), out.ctypes.data_as(C.POINTER(C.c_double))) == \
+        abi.MHD_ERR_NUMERIC
+    rk, drk, walls = np.empty(case.nz), np.empty(case.nz), np.empty(3)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    assert L.mhd_static_lrem_profile(C.byref(p), C.byref(sp), dp(rk), dp(drk), dp(walls)) == abi.MHD_ERR_NUMERIC
+    refcase = pytest.importorskip("refcase")
+    if not refcase.reference_available():
+        return
+    with pytest.raises(RuntimeError, match="Stepsize not significant in RKQC"):
+        refcase.run(case, {k: np.zeros(case.shape) for k in STATE_FIELDS}, "static", 0, timeout=300)
