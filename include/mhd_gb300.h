@@ -350,6 +350,9 @@ int mhd_batch_steps(mhd_batch* b, int nsteps);
  * its count drops out of the work list for the rest of the call, so a
  * server's quantum need not shrink to the shortest remaining request. */
 int mhd_batch_steps_limited(mhd_batch* b, int nsteps, const int* max_steps);
+/* Wait for the batch's queued steps.  The kernels check every work item
+ * against its instance's grid before using it; an item that fails is skipped
+ * and reported here as MHD_ERR_INVALID (details on stderr). */
 int mhd_batch_sync(mhd_batch* b);
 
 /* ---- device selection and timing ---------------------------------------- */
