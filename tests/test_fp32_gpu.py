@@ -1,7 +1,9 @@
 """FP32-storage form: fields stored and stenciled in FP32 (RO and TT as
-deviations from FP64 reference profiles), pressure/gravity, the RK3
-register and the reductions in FP64.  Checked against the FP64 paths."""
+deviations from FP64 reference profiles); the equation of state, the
+profiles' hydrostatic residual, the RK3 register and the reductions in FP64.
+Checked against the oracle and the FP64 paths."""
 import ctypes as C
+import itertools
 
 import numpy as np
 import pytest
@@ -46,6 +48,47 @@ def test_one_step_close_to_fp64(name):
     o.steps(1)
     for k in STATE_FIELDS[:case.nfields]:
         assert rel_err(got[k], o.arr[k]) <= 1e-5, (k, rel_err(got[k], o.arr[k]))
+
+
+@pytest.mark.parametrize("mag,rot,shr", list(itertools.product([True, False], [True, False], [True, False])))
+def test_one_step_all_switch_sets_fp32(mag, rot, shr):
+    """Every lMag / lRot / lShr combination with FP32 storage, one step
+    against the oracle: 1e-5 of each field's max-norm."""
+    case = small_cases()["mhd_fixedT"].replace(lMag=mag, lRot=rot, lShr=shr, ANG=0.3, nPx=20, nPy=12, nPz=10)
+    st = initial_state(case)
+    sim = Simulation(case, precision="fp32")
+    sim.upload_state(st)
+    sim.communicate()
+    sim.step(case.dt)
+    got = sim.download_state()
+    sim.close()
+    o = oracle_for(case, st)
+    o.steps(1)
+    for k in STATE_FIELDS[:case.nfields]:
+        assert rel_err(got[k], o.arr[k]) <= 1e-5, (k, rel_err(got[k], o.arr[k]))
+
+
+def test_headline_physics_100_steps_l2_error(capsys):
+    """lMag + lRot (0.1 about z) + lShr at 64x64x32, 100 steps: FP32 storage
+    (with lShr's persistent FP64 temperature right-hand side) against the FP64
+    fused path, every field within 1e-5 relative L2."""
+    from mhd_gb300.case import config1
+    case = config1().replace(nPx=64, nPy=64, nPz=32, noise=1e-2, name="config1_physics_64x64x32")
+    st = initial_state(case)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        sim = Simulation(case, precision=prec)
+        sim.upload_state(st)
+        sim.communicate()
+        sim.steps(100, case.dt)
+        res[prec] = sim.download_state()
+        sim.close()
+    errs = {k: l2_rel(res["fp32"][k], res["fp64"][k]) for k in STATE_FIELDS}
+    with capsys.disabled():
+        print("\nFP32-storage vs FP64, lMag+lRot+lShr 64x64x32, 100 steps, relative L2:",
+              {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v <= 1e-5, (k, v)
 
 
 def test_ghost_images_exact_in_fp32():
