@@ -134,8 +134,8 @@ class Server:
         self.tuned = {"fp64": tile is not None, "fp32": False}
         self.zrange = {"fp64": None, "fp32": None}
         self.balance = balance
-        # nominal cell-RK3-updates/s of a batch per precision (measured, 64-instance batch)
-        self.rates = dict(rates or {"fp64": 7.9e8, "fp32": 3.0e9})
+        # nominal cell-RK3-updates/s of a batch per precision (the 64-instance batch, measured)
+        self.rates = dict(rates or {"fp64": 8.0e8, "fp32": 3.5e9})
         self.progress = progress
         self.progress_s = float(progress_s)
         self.completed = 0
