@@ -415,7 +415,9 @@ int autotune(mhd_batch* b, double* ms_out) {
             cudaMemcpyAsync(d_args, args.data(), sizeof(FusedArgs) * args.size(), cudaMemcpyHostToDevice, b->stream);
             cudaStreamSynchronize(b->stream);
         }
-        // every instance steps in every timed step
+        // every instance steps in every timed step (the staging buffer is reused:
+        // a call's steps may still be waiting to read it)
+        cudaEventSynchronize(b->left_copied);
         for (int i = 0; i < n; i++) b->h_left[i] = kNoLimit;
         cudaMemcpyAsync(b->d_left, b->h_left, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream);
         cudaEventRecord(b->left_copied, b->stream);
