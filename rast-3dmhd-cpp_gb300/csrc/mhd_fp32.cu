@@ -413,14 +413,26 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
             // substage (and a halted record) stores U' itself into Z; the split
             // keeps its unused register update off the FP64 pipe.
             auto epilogue = [&](auto next_register) {
+                // the register fields are read four at a time before any of the
+                // four is written: the stores may alias the loads as far as the
+                // compiler knows, so a load after a store would wait for it
 #pragma unroll
-                for (int f = 0; f < 8; f++) {
-                    if (f >= nf) break;
-                    const double zf = a.Z.p[f][i];
-                    const double un = halted ? zf : fma(gdt, fl[f], zf);
-                    const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
-                    store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
-                    a.Z.p[f][i] = next_register ? fma(zdt, fl[f], un) : un;
+                for (int f0 = 0; f0 < 8; f0 += 4) {
+                    if (f0 >= nf) break;
+                    double zv[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (f0 + j < nf) zv[j] = a.Z.p[f0 + j][i];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int f = f0 + j;
+                        if (f >= nf) break;
+                        const double zf = zv[j];
+                        const double un = halted ? zf : fma(gdt, fl[f], zf);
+                        const double prof = (f == S_TT) ? t0z : (f == S_RO) ? r0z : 0.0;
+                        store32_with_images(a.Uo.p[f], g, z, y, x, narrow_f64(un - prof));
+                        a.Z.p[f][i] = next_register ? fma(zdt, fl[f], un) : un;
+                    }
                 }
             };
             if (a.substage < 2 && !halted) epilogue(std::true_type{});
