@@ -529,6 +529,19 @@ struct CflFields64 {
     // the estimate's float input of field k (truncated to 23 bits) and whether it is nonzero
     __device__ float fe(int k, long long i) const { return trunc_to_f32(U.p[k][i]); }
     __device__ bool nz(int k, long long i) const { return nonzero_bits(U.p[k][i]); }
+    // Estimate inputs ro, tt of a filtered row (truncated to 23 bits: relative
+    // error below 2^-23) and m, the value whose row minimum gives the row's
+    // smallest ro: here ro itself.
+    struct Row {};
+    using Min = double;
+    __device__ Row row(int) const { return {}; }
+    __device__ void est_in(const Row&, long long i, float& ro, float& tt, bool& ok, double& m) const {
+        m = U.p[S_RO][i];
+        ro = trunc_to_f32(m);
+        tt = trunc_to_f32(U.p[S_TT][i]);
+        ok = true;
+    }
+    __device__ double ro_min(double m, int) const { return m; }
 };
 struct CflFields32 {
     Fields8f U;
@@ -539,6 +552,25 @@ struct CflFields32 {
     // stored floats are their own estimate input (exact; subnormals kept)
     __device__ float fe(int k, long long i) const { return U.p[k][i]; }
     __device__ bool nz(int k, long long i) const { return (__float_as_uint(U.p[k][i]) & 0x7fffffffu) != 0u; }
+    // Estimate inputs of a filtered row, with no FP64 operation per cell:
+    // ro = float(rho0) + dro and tt = float(T0) + dT in FP32.  Against the FP64
+    // values their relative error is at most 5 * 2^-24 (the profile's rounding,
+    // amplified at most 4 times by cancellation, plus the sum's own), which
+    // `ok` requires by |float(rho0)| <= 4 |ro| and |float(T0)| <= 4 |tt|.
+    // m = dro: rho0 + dro rounds monotonically in dro, so the row's smallest
+    // ro is rho0 plus its smallest dro, one FP64 sum per row.
+    struct Row {
+        float Rf, Tf;
+    };
+    using Min = float;
+    __device__ Row row(int z) const { return {narrow_f64(bgR[z]), narrow_f64(bgT[z])}; }
+    __device__ void est_in(const Row& r, long long i, float& ro, float& tt, bool& ok, float& m) const {
+        m = U.p[S_RO][i];
+        ro = __fadd_rn(r.Rf, m);
+        tt = __fadd_rn(r.Tf, U.p[S_TT][i]);
+        ok = fabsf(r.Rf) <= 4.0f * fabsf(ro) && fabsf(r.Tf) <= 4.0f * fabsf(tt);
+    }
+    __device__ double ro_min(float m, int z) const { return bgR[z] + widen_f32(m); }
 };
 
 // mc and the fast-mode speed^2 UU' of cell i (plane z)
@@ -607,14 +639,16 @@ __device__ void write_cfl_partials(double um, double w0, double w1, double w2, d
 }
 
 
-// FP32 estimates of cell i's fast-mode candidate a0 and of mc (both certified
-// to 1.2e-6 when `ok`), and whether its momenta are not all exactly zero.
+// FP32 estimates of cell i's fast-mode candidate a0 and of mc from the float
+// inputs ro, tt (certified by `okin`), and whether its momenta are not all
+// exactly zero.  When `ok`, both are certified to 1.4e-6: to first order in
+// u = 2^-24, mc is within 18u (inputs truncated to 23 bits) or 23u (FP32
+// storage: exact momenta and fields, ro and tt within 5u), a0 within 16u.
 template <bool MAG, class FA>
-__device__ __forceinline__ void cfl_estimate(const FA& U, long long i, int z, float ddf, float gam_f, float obeta_f,
-                                             double rod, float& a0, float& mc, bool& ok, bool& nz) {
+__device__ __forceinline__ void cfl_estimate(const FA& U, long long i, float ro, float tt, bool okin, float ddf,
+                                             float gam_f, float obeta_f, float& a0, float& mc, bool& ok, bool& nz) {
     const float ru = U.fe(S_RU, i), rv = U.fe(S_RV, i), rw = U.fe(S_RW, i);
     nz = U.nz(S_RU, i) | U.nz(S_RV, i) | U.nz(S_RW, i);  // no short circuit: the loads stay unconditional
-    const float ro = trunc_to_f32(rod), tt = trunc_to_f32(U.tt(i, z));
     const float ir = __frcp_rn(ro);
     const float sq = __fadd_rn(__fadd_rn(__fmul_rn(ru, ru), __fmul_rn(rv, rv)), __fmul_rn(rw, rw));
     const float uuk = __fmul_rn(__fmul_rn(sq, ir), ir);
@@ -627,7 +661,7 @@ __device__ __forceinline__ void cfl_estimate(const FA& U, long long i, int z, fl
     const float uuf = __fadd_rn(__fadd_rn(uuk, G), __fmul_rn(2.0f, __fsqrt_rn(__fmul_rn(uuk, G))));
     mc = __fdiv_rn(uuk, tt);
     a0 = __fmul_rn(ddf, rsqrtf(uuf));
-    ok = (ro >= 0x1p-20f && ro <= 0x1p20f) && (tt >= 0x1p-20f && tt <= 0x1p20f) && isfinite(uuf) &&
+    ok = okin && (ro >= 0x1p-20f && ro <= 0x1p20f) && (tt >= 0x1p-20f && tt <= 0x1p20f) && isfinite(uuf) &&
          isfinite(mc) && isfinite(a0);
 }
 
@@ -640,6 +674,31 @@ __device__ __forceinline__ bool cfl_fast_row(const Grid& g, const Consts& c, int
     return consts_ok && (g.nx <= 3 || !(c.DDXmin < DDyz)) && P1 > 0.0 && P2 > 0.0 && cfl_kappa(c, z) > 0.0;
 }
 
+// A row's place, DD and filter test.  A warp works through its rows in batches
+// of 32, lane j evaluating the j-th row's FP64 scalars and handing them to the
+// others by shuffle: GB300's FP64 pipe retires about 2 lanes per clock per SM,
+// so a warp-uniform FP64 expression costs as much as 32 distinct ones.
+struct CflRowInfo {
+    int y, z;
+    double DD;
+    bool fast;
+};
+// row r (of nPy x nPz, y fastest) when r < nrows; otherwise not fast
+__device__ __forceinline__ CflRowInfo cfl_row_info(const Grid& g, const Consts& c, long long r, long long nrows) {
+    CflRowInfo ri{1, 1, 0.0, false};
+    if (r < nrows) {
+        const int nPy = g.ny - 2;
+        ri.y = 1 + (int)(r % nPy);
+        ri.z = 1 + (int)(r / nPy);
+        ri.fast = cfl_fast_row(g, c, ri.y, ri.z, ri.DD);
+    }
+    return ri;
+}
+__device__ __forceinline__ CflRowInfo cfl_row_from(const CflRowInfo& a, int t) {
+    return {__shfl_sync(0xffffffffu, a.y, t), __shfl_sync(0xffffffffu, a.z, t), __shfl_sync(0xffffffffu, a.DD, t),
+            __shfl_sync(0xffffffffu, (int)a.fast, t) != 0};
+}
+
 // Seeds of the filter: the smallest a0 estimate and the largest mc estimate
 // (momenta not all zero) over every kCflSeedStride-th row, as ordered integer
 // keys (0 = nothing seen).  Any estimate that some certified cell attains is a
@@ -648,26 +707,33 @@ constexpr int kCflSeedStride = 8;
 template <bool MAG, class FA>
 __global__ void k_cfl_seed(Grid g, Consts c, FA U, unsigned* seed) {
     const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
-    const long long nrows = ((long long)nPy * nPz + kCflSeedStride - 1) / kCflSeedStride;
+    const long long nall = (long long)nPy * nPz;
+    const long long nrows = (nall + kCflSeedStride - 1) / kCflSeedStride;
     const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * blockDim.x / 32;
     const float gam_f = (float)c.GAMMA, obeta_f = (float)c.OBETA;
     float best_a = INFINITY, best_m = 0.0f;
-    for (long long q = (long long)(blockIdx.x * blockDim.x + threadIdx.x) / 32; q < nrows;
-         q += (long long)gridDim.x * blockDim.x / 32) {
-        const long long r = q * kCflSeedStride;
-        const int y = 1 + (int)(r % nPy), z = 1 + (int)(r / nPy);
-        double DDyz;
-        if (!cfl_fast_row(g, c, y, z, DDyz)) continue;
-        const float ddf = narrow_f64(DDyz);
-        const long long row = (long long)z * g.sz + (long long)y * g.sy;
+    for (long long qb = (long long)(blockIdx.x * blockDim.x + threadIdx.x) / 32; qb < nrows; qb += 32 * warps) {
+        const long long qj = qb + lane * warps;
+        const CflRowInfo mine = cfl_row_info(g, c, qj < nrows ? qj * kCflSeedStride : nall, nall);
+        for (int t = 0; t < 32 && qb + t * warps < nrows; t++) {
+            const CflRowInfo ri = cfl_row_from(mine, t);
+            if (!ri.fast) continue;
+            const int y = ri.y, z = ri.z;
+            const float ddf = narrow_f64(ri.DD);
+            const long long row = (long long)z * g.sz + (long long)y * g.sy;
+            const typename FA::Row rk = U.row(z);
 #pragma unroll 4
-        for (int x = 1 + lane; x <= nPx; x += 32) {  // unrolled: the cells' loads overlap
-            float a0, mc;
-            bool ok, nz;
-            cfl_estimate<MAG>(U, row + x, z, ddf, gam_f, obeta_f, U.ro(row + x, z), a0, mc, ok, nz);
-            if (ok) {
-                best_a = fminf(best_a, a0);
-                if (nz) best_m = fmaxf(best_m, mc);
+            for (int x = 1 + lane; x <= nPx; x += 32) {  // unrolled: the cells' loads overlap
+                float ro, tt, a0, mc;
+                bool okin, ok, nz;
+                typename FA::Min m;
+                U.est_in(rk, row + x, ro, tt, okin, m);
+                cfl_estimate<MAG>(U, row + x, ro, tt, okin, ddf, gam_f, obeta_f, a0, mc, ok, nz);
+                if (ok) {
+                    best_a = fminf(best_a, a0);
+                    if (nz) best_m = fmaxf(best_m, mc);
+                }
             }
         }
     }
@@ -694,10 +760,11 @@ constexpr float kCflTau = 1.52587890625e-05f;    // 2^-16: filter margin, > 2x t
 // per-cell FP64 arithmetic except where they can decide the result:
 //   * a1, a2 are products/quotients of ro with positive row constants and a3
 //     depends on DD alone; rounding is monotone, so their row minima are the
-//     candidates of the row's smallest ro (an exact FP64 min);
+//     candidates of the row's smallest ro (an exact min: of ro in FP64, of the
+//     stored deviation with FP32 storage);
 //   * mc and a0 = DD/sqrt(UU') are estimated in FP32 from inputs truncated to
-//     23 bits, or read as stored with FP32 storage (error below 1.2e-6 for
-//     inputs in the accepted ranges); a cell is
+//     23 bits, or from the stored floats with ro and T summed in FP32 with
+//     FP32 storage (error below 1.4e-6 for inputs in the accepted ranges); a cell is
 //     evaluated exactly when its estimate lies within 2^-16 of the best
 //     estimate the warp has seen so far (the running maximum of mc, minimum of
 //     a0, the current pass included), or when its estimate is not certified
@@ -722,83 +789,95 @@ __global__ void __launch_bounds__(kCflWarps * 32, 3) k_cfl_rows(Grid g, Consts c
     // the best estimates so far (warp-uniform), starting from the seeds
     float run_a = seed[0] ? __uint_as_float(0x7f800000u - seed[0]) : INFINITY;
     float run_m = seed[1] ? __uint_as_float(seed[1]) : -INFINITY;
-    for (long long r = (long long)blockIdx.x * kCflWarps + wid; r < nrows; r += (long long)gridDim.x * kCflWarps) {
-        const int y = 1 + (int)(r % nPy), z = 1 + (int)(r / nPy);
-        const long long row = (long long)z * g.sz + (long long)y * g.sy;
-        double DDyz;
-        const bool fast = cfl_fast_row(g, c, y, z, DDyz);
-        if (!fast) {
-            for (int x = 1 + lane; x <= nPx; x += 32) cfl_cell<MAG>(g, c, U, x, y, z, OGAMMA, um, w0, w1, w2, w3);
-            continue;
-        }
-        double mro = __longlong_as_double(0x7ff0000000000000LL);  // +inf: no cell yet
-        const float ddf = narrow_f64(DDyz);
-        for (int x0 = 1; x0 <= nPx; x0 += 32 * kCflK) {
-            float aA[kCflK], mA[kCflK];
-            unsigned okm = 0u, nzm = 0u, valid = 0u;
-            float Ma = INFINITY, Mm = -INFINITY;
+    const long long stride = (long long)gridDim.x * kCflWarps;
+    for (long long rb = (long long)blockIdx.x * kCflWarps + wid; rb < nrows; rb += 32 * stride) {
+        // lane j holds the j-th row of this batch of 32 and, once that row is
+        // reduced, its smallest density (stored deviation with FP32 storage)
+        const CflRowInfo mine = cfl_row_info(g, c, rb + lane * stride, nrows);
+        typename FA::Min mine_ro = INFINITY;
+        for (int t = 0; t < 32 && rb + t * stride < nrows; t++) {
+            const CflRowInfo ri = cfl_row_from(mine, t);
+            const int y = ri.y, z = ri.z;
+            const long long row = (long long)z * g.sz + (long long)y * g.sy;
+            if (!ri.fast) {
+                for (int x = 1 + lane; x <= nPx; x += 32) cfl_cell<MAG>(g, c, U, x, y, z, OGAMMA, um, w0, w1, w2, w3);
+                continue;
+            }
+            const double DDyz = ri.DD;
+            typename FA::Min mro = INFINITY;  // no cell yet
+            const float ddf = narrow_f64(DDyz);
+            const typename FA::Row rk = U.row(z);
+            for (int x0 = 1; x0 <= nPx; x0 += 32 * kCflK) {
+                float aA[kCflK], mA[kCflK];
+                unsigned okm = 0u, nzm = 0u, valid = 0u;
+                float Ma = INFINITY, Mm = -INFINITY;
 #pragma unroll
-            for (int k = 0; k < kCflK; k++) {
-                const int x = x0 + k * 32 + lane;
-                aA[k] = 0.0f;
-                mA[k] = 0.0f;
-                if (x > nPx) continue;
-                valid |= 1u << k;
-                const long long i = row + x;
-                const double rod = U.ro(i, z);
-                mro = (rod < mro) ? rod : mro;
-                float a0, mc;
-                bool ok, nz;
-                cfl_estimate<MAG>(U, i, z, ddf, gam_f, obeta_f, rod, a0, mc, ok, nz);
-                aA[k] = a0;
-                mA[k] = mc;
-                if (ok) {
-                    okm |= 1u << k;
-                    Ma = fminf(Ma, a0);
-                    if (nz) Mm = fmaxf(Mm, mc);
+                for (int k = 0; k < kCflK; k++) {
+                    const int x = x0 + k * 32 + lane;
+                    aA[k] = 0.0f;
+                    mA[k] = 0.0f;
+                    if (x > nPx) continue;
+                    valid |= 1u << k;
+                    const long long i = row + x;
+                    float ro, tt, a0, mc;
+                    bool okin, ok, nz;
+                    typename FA::Min m;
+                    U.est_in(rk, i, ro, tt, okin, m);
+                    mro = (m < mro) ? m : mro;
+                    cfl_estimate<MAG>(U, i, ro, tt, okin, ddf, gam_f, obeta_f, a0, mc, ok, nz);
+                    aA[k] = a0;
+                    mA[k] = mc;
+                    if (ok) {
+                        okm |= 1u << k;
+                        Ma = fminf(Ma, a0);
+                        if (nz) Mm = fmaxf(Mm, mc);
+                    }
+                    if (nz) nzm |= 1u << k;
                 }
-                if (nz) nzm |= 1u << k;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    Ma = fminf(Ma, __shfl_xor_sync(0xffffffffu, Ma, o));
+                    Mm = fmaxf(Mm, __shfl_xor_sync(0xffffffffu, Mm, o));
+                }
+                run_a = fminf(run_a, Ma);
+                run_m = fmaxf(run_m, Mm);
+                const float ta = run_a + kCflTau * run_a;
+                const float tm = (run_m >= 0x1p-40f) ? run_m - kCflTau * run_m : -INFINITY;
+                int n = 0;
+#pragma unroll
+                for (int k = 0; k < kCflK; k++) {
+                    const bool v = (valid >> k) & 1u, ok = (okm >> k) & 1u, nz = (nzm >> k) & 1u;
+                    const bool cand = v && (!ok || aA[k] <= ta || (nz && mA[k] >= tm));
+                    const unsigned bal = __ballot_sync(0xffffffffu, cand);
+                    if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
+                    n += __popc(bal);
+                }
+                __syncwarp();
+                for (int j = lane; j < n; j += 32) {
+                    const int x = list[wid][j];
+                    double mc, UU;
+                    cfl_speeds<MAG>(c, U, row + x, z, OGAMMA, mc, UU);
+                    um = (um < mc) ? mc : um;
+                    const double a0 = DDyz / sqrt(UU);
+                    w0 = (a0 < w0) ? a0 : w0;
+                }
+                __syncwarp();
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                Ma = fminf(Ma, __shfl_xor_sync(0xffffffffu, Ma, o));
-                Mm = fmaxf(Mm, __shfl_xor_sync(0xffffffffu, Mm, o));
+                const typename FA::Min q = __shfl_xor_sync(0xffffffffu, mro, o);
+                mro = (q < mro) ? q : mro;
             }
-            run_a = fminf(run_a, Ma);
-            run_m = fmaxf(run_m, Mm);
-            const float ta = run_a + kCflTau * run_a;
-            const float tm = (run_m >= 0x1p-40f) ? run_m - kCflTau * run_m : -INFINITY;
-            int n = 0;
-#pragma unroll
-            for (int k = 0; k < kCflK; k++) {
-                const bool v = (valid >> k) & 1u, ok = (okm >> k) & 1u, nz = (nzm >> k) & 1u;
-                const bool cand = v && (!ok || aA[k] <= ta || (nz && mA[k] >= tm));
-                const unsigned bal = __ballot_sync(0xffffffffu, cand);
-                if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
-                n += __popc(bal);
-            }
-            __syncwarp();
-            for (int j = lane; j < n; j += 32) {
-                const int x = list[wid][j];
-                double mc, UU;
-                cfl_speeds<MAG>(c, U, row + x, z, OGAMMA, mc, UU);
-                um = (um < mc) ? mc : um;
-                const double a0 = DDyz / sqrt(UU);
-                w0 = (a0 < w0) ? a0 : w0;
-            }
-            __syncwarp();
+            if (lane == t) mine_ro = mro;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double q = __shfl_xor_sync(0xffffffffu, mro, o);
-            mro = (q < mro) ? q : mro;
-        }
-        if (lane == 0) {
-            const double a1 = cfl_a1(c, DDyz, mro, z), a2 = cfl_a2(c, DDyz, mro);
+        // the a1..a3 candidates of every fast row of the batch, one row per lane
+        if (mine.fast) {
+            const double rmin = U.ro_min(mine_ro, mine.z);
+            const double a1 = cfl_a1(c, mine.DD, rmin, mine.z), a2 = cfl_a2(c, mine.DD, rmin);
             w1 = (a1 < w1) ? a1 : w1;
             w2 = (a2 < w2) ? a2 : w2;
             if constexpr (MAG) {
-                const double a3 = cfl_a3(c, DDyz);
+                const double a3 = cfl_a3(c, mine.DD);
                 w3 = (a3 < w3) ? a3 : w3;
             }
         }

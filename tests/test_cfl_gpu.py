@@ -237,14 +237,16 @@ def test_cfl_reduction_after_fused_steps():
     assert got == want
 
 
-@pytest.mark.parametrize("kind", ["run", "ties", "tiny_and_odd"])
+@pytest.mark.parametrize("kind", ["run", "ties", "tiny_and_odd", "cancel", "guard_edge"])
 def test_fp32_cfl_reduction_bit_exact(kind):
-    """FP32 storage: the filtered reduction reads the stored floats as its
-    estimates and reduces the widened FP64 state (profile + deviation) exactly;
-    DT and UMACH equal the oracle's cell-by-cell reduction over the state
-    mhd_download_state returns (the same FP64 values), bit for bit, for an
-    evolved flow, a state of ties, and tiny, subnormal-float, huge and
-    negative values."""
+    """FP32 storage: the filtered reduction estimates from the stored floats
+    (ro and T summed with the profile in FP32) and reduces the widened FP64
+    state (profile + deviation) exactly; DT and UMACH equal the oracle's
+    cell-by-cell reduction over the state mhd_download_state returns (the same
+    FP64 values), bit for bit, for an evolved flow, a state of ties, tiny,
+    subnormal-float, huge and negative values, and the fastest cells where
+    density or temperature fall far below the profile (the FP32 sum cancels:
+    not certified) or just inside and outside the 4:1 cancellation bound."""
     case = Case(nPx=70, nPy=36, nPz=20, lMag=True, lRot=True, seed=12, noise=1e-2, name="cfl32x")
     sim = Simulation(case, precision="fp32")
     if kind == "run":
@@ -259,6 +261,17 @@ def test_fp32_cfl_reduction_bit_exact(kind):
             st["RU"][...] = 0.01
             st["RV"][...] = -0.02
             st["RW"][...] = 0.0
+        elif kind == "cancel":
+            # momenta keep the unscaled density, so these cells are the fastest
+            st = _random_flow(case, 6, 3e-2)
+            st["RO"][8:11, 10:14, 20:30] *= 0.05
+            st["TT"][4:6, 20:22, 50:60] *= 0.1
+        elif kind == "guard_edge":
+            st = _random_flow(case, 7, 3e-2)
+            st["RO"][3:6, 5:9, 10:20] *= 0.26             # profile / density about 3.8: estimated
+            st["RO"][14:17, 25:29, 40:50] *= 0.24         # about 4.2: evaluated exactly
+            st["TT"][10:12, 15:18, 30:35] *= 0.26
+            st["TT"][16:18, 2:5, 60:66] *= 0.24
         else:
             st = _random_flow(case, 5, 1e-25)
             st["RU"][7, 9, 11] = 3e-3                  # one real flow cell
