@@ -703,7 +703,7 @@ __device__ __forceinline__ CflRowInfo cfl_row_from(const CflRowInfo& a, int t) {
 // (momenta not all zero) over every kCflSeedStride-th row, as ordered integer
 // keys (0 = nothing seen).  Any estimate that some certified cell attains is a
 // valid filter base, so the row kernel may start from these.
-constexpr int kCflSeedStride = 8;
+constexpr int kCflSeedStride = 16;
 template <bool MAG, class FA>
 __global__ void k_cfl_seed(Grid g, Consts c, FA U, unsigned* seed) {
     const int nPx = g.nx - 2, nPy = g.ny - 2, nPz = g.nz - 2;
@@ -843,25 +843,35 @@ __global__ void __launch_bounds__(kCflWarps * 32, 3) k_cfl_rows(Grid g, Consts c
                 run_m = fmaxf(run_m, Mm);
                 const float ta = run_a + kCflTau * run_a;
                 const float tm = (run_m >= 0x1p-40f) ? run_m - kCflTau * run_m : -INFINITY;
-                int n = 0;
+                unsigned cm = 0u;  // this lane's cells to evaluate exactly, bit k
 #pragma unroll
                 for (int k = 0; k < kCflK; k++) {
                     const bool v = (valid >> k) & 1u, ok = (okm >> k) & 1u, nz = (nzm >> k) & 1u;
-                    const bool cand = v && (!ok || aA[k] <= ta || (nz && mA[k] >= tm));
-                    const unsigned bal = __ballot_sync(0xffffffffu, cand);
-                    if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
-                    n += __popc(bal);
+                    if (v && (!ok || aA[k] <= ta || (nz && mA[k] >= tm))) cm |= 1u << k;
                 }
-                __syncwarp();
-                for (int j = lane; j < n; j += 32) {
-                    const int x = list[wid][j];
-                    double mc, UU;
-                    cfl_speeds<MAG>(c, U, row + x, z, OGAMMA, mc, UU);
-                    um = (um < mc) ? mc : um;
-                    const double a0 = DDyz / sqrt(UU);
-                    w0 = (a0 < w0) ? a0 : w0;
+                // Most passes have no such cell; the compaction (ballots and
+                // population counts, the latter on GB300's FP64 pipe) runs
+                // only when one has.
+                if (__any_sync(0xffffffffu, cm != 0u)) {
+                    int n = 0;
+#pragma unroll
+                    for (int k = 0; k < kCflK; k++) {
+                        const bool cand = (cm >> k) & 1u;
+                        const unsigned bal = __ballot_sync(0xffffffffu, cand);
+                        if (cand) list[wid][n + __popc(bal & ((1u << lane) - 1u))] = x0 + k * 32 + lane;
+                        n += __popc(bal);
+                    }
+                    __syncwarp();
+                    for (int j = lane; j < n; j += 32) {
+                        const int x = list[wid][j];
+                        double mc, UU;
+                        cfl_speeds<MAG>(c, U, row + x, z, OGAMMA, mc, UU);
+                        um = (um < mc) ? mc : um;
+                        const double a0 = DDyz / sqrt(UU);
+                        w0 = (a0 < w0) ? a0 : w0;
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
