@@ -270,12 +270,20 @@ int profiles_from_means(mhd_ctx* ctx) {
         double hz = 0.0;
         if (z > 0 && z < nz - 1) hz = r0[z] * ctx->prm.GRAV - (r0[z + 1] * bg[z + 1] - r0[z - 1] * bg[z - 1]) * cz1[z];
         ctx->h_zf[7 * (size_t)nz + z] = (float)hz;
+        // rho0 and T0 as float pairs hi + lo (hi the nearest float, lo the
+        // nearest float to the exact remainder): about 48 significant bits,
+        // for the FP32 kernels' compensated reconstruction of rho and p
+        const float rh = (float)r0[z], th = (float)bg[z];
+        ctx->h_zf[8 * (size_t)nz + z] = rh;
+        ctx->h_zf[9 * (size_t)nz + z] = (float)(r0[z] - (double)rh);
+        ctx->h_zf[10 * (size_t)nz + z] = th;
+        ctx->h_zf[11 * (size_t)nz + z] = (float)(bg[z] - (double)th);
     }
     // on the context's stream: its kernels read the profiles (a plain cudaMemcpy
     // runs on the legacy stream, which the non-blocking context stream does not
     // wait for); the sync keeps h_bg / h_zf stable until the copies are done
     CK(cudaMemcpyAsync(ctx->d_bg, ctx->h_bg.data(), sizeof(double) * 4 * nz, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 8 * nz, cudaMemcpyHostToDevice,
+    CK(cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * kZfRows * nz, cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return MHD_OK;
@@ -687,16 +695,17 @@ int mhd_create(const mhd_params* params, void* stream, mhd_ctx** out) {
     int arc = MHD_OK;
     if (ctx->fp32) {
         arc = alloc_f32(ctx, &ctx->U32[0]);
-        // 4 x nz double profiles, then the [8][nz] float coefficient table (8 x nz doubles in all)
-        if (!arc && cudaMalloc(&ctx->d_bg, sizeof(double) * 8 * nz) != cudaSuccess) arc = MHD_ERR_NOMEM;
-        if (!arc && cudaMemsetAsync(ctx->d_bg, 0, sizeof(double) * 8 * nz, ctx->stream) != cudaSuccess) arc = MHD_ERR_CUDA;
-        ctx->h_zf.assign(8 * (size_t)nz, 0.0f);
+        // 4 x nz double profiles, then the [kZfRows][nz] float coefficient table
+        const size_t bg_bytes = sizeof(double) * 4 * nz + sizeof(float) * kZfRows * nz;
+        if (!arc && cudaMalloc(&ctx->d_bg, bg_bytes) != cudaSuccess) arc = MHD_ERR_NOMEM;
+        if (!arc && cudaMemsetAsync(ctx->d_bg, 0, bg_bytes, ctx->stream) != cudaSuccess) arc = MHD_ERR_CUDA;
+        ctx->h_zf.assign(kZfRows * (size_t)nz, 0.0f);
         for (int z = 0; z < nz; z++) {
             for (int r = 0; r < 3; r++) ctx->h_zf[(size_t)r * nz + z] = (float)ctx->h_cz[(size_t)r * nz + z];
             ctx->h_zf[5 * (size_t)nz + z] = (float)p.RKAPA[z];
             ctx->h_zf[6 * (size_t)nz + z] = (float)p.DKAPA[z];
         }
-        if (!arc && cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * 8 * nz,
+        if (!arc && cudaMemcpyAsync(ctx->d_bg + 4 * nz, ctx->h_zf.data(), sizeof(float) * kZfRows * nz,
                                     cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) arc = MHD_ERR_CUDA;
     } else {
         arc = alloc_block(ctx, &ctx->U[0], 8);

@@ -229,6 +229,8 @@ int fused_bcon_wall(unsigned sw, const Grid& g, const Consts& c, Fields8 U, doub
 struct Fields8f {
     float* p[8];
 };
+// rows of the FP32 kernels' per-z float table (Fused32Args::zf)
+constexpr int kZfRows = 12;
 struct Fused32Args {
     Grid g;
     Consts c;
@@ -239,8 +241,9 @@ struct Fused32Args {
     double* FT;    // FP64 persistent temperature right-hand side (lShr only)
     const double *bgR, *bgT;     // reference profiles rho0(z), T0(z)
     const double *dzT0, *d2zT0;  // their premultiplied first and second z derivatives
-    const float* zf;             // [8][nz] float cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA, and the
-                                 // profiles' hydrostatic residual rho0 GRAV - D_z(rho0 T0)
+    const float* zf;             // [kZfRows][nz] float cz1, cz2a, cz2b, dzT0, d2zT0, RKAPA, DKAPA, the
+                                 // profiles' hydrostatic residual rho0 GRAV - D_z(rho0 T0), and
+                                 // rho0, T0 as float pairs (rows 8, 9 and 10, 11: hi, lo)
     double gdt, zdt;
     double timt;
     int substage;

@@ -42,12 +42,13 @@ struct mhd_ctx {
     bool fp32 = false;
     float* U32[2] = {nullptr, nullptr};
     double* FT64 = nullptr;     // persistent FT (lShr)
-    double* d_bg = nullptr;     // rho0, T0, dzT0, d2zT0 (4 x nz)
+    double* d_bg = nullptr;     // rho0, T0, dzT0, d2zT0 (4 x nz), then the float table
     std::vector<double> h_bg;   // host copy of the four profiles
     std::vector<double> h_cz;   // cz1, cz2a, cz2b (3 x nz)
-    // float per-z coefficients of the FP32 kernels, [8][nz]: cz1, cz2a, cz2b,
-    // dzT0, d2zT0, RKAPA, DKAPA and the profiles' hydrostatic residual
-    // rho0 GRAV - D_z(rho0 T0) (device copy after d_bg's 4 x nz doubles)
+    // float per-z coefficients of the FP32 kernels, [kZfRows][nz]: cz1, cz2a,
+    // cz2b, dzT0, d2zT0, RKAPA, DKAPA, the profiles' hydrostatic residual
+    // rho0 GRAV - D_z(rho0 T0), and rho0, T0 as float pairs hi, lo (device
+    // copy after d_bg's 4 x nz doubles)
     std::vector<float> h_zf;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     bool profiling = false;

