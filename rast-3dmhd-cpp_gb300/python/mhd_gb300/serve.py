@@ -134,8 +134,9 @@ class Server:
         self.tuned = {"fp64": tile is not None, "fp32": False}
         self.zrange = {"fp64": None, "fp32": None}
         self.balance = balance
-        # nominal cell-RK3-updates/s of a batch per precision (the 64-instance batch, measured)
-        self.rates = dict(rates or {"fp64": 8.0e8, "fp32": 3.5e9})
+        # nominal cell-RK3-updates/s of a batch per precision (the 64-instance batch, measured:
+        # 7.97e8 and 4.29e9)
+        self.rates = dict(rates or {"fp64": 8.0e8, "fp32": 4.3e9})
         self.progress = progress
         self.progress_s = float(progress_s)
         self.completed = 0
@@ -223,7 +224,7 @@ class Server:
         estimated step (cells / nominal rate of its precision) takes `quantum`
         steps; with balance on, every other batch takes as many steps as fit
         in the same time (at most 8 x quantum), so the FP32-storage batch,
-        about four times faster per cell, does not idle while the FP64 batch
+        about five times faster per cell, does not idle while the FP64 batch
         finishes its quantum."""
         est = {key: sum(self.resident[rid].req.case.cells for rid in rids) / self.rates[key[0]]
                for key, rids in self.batch_members.items()}
