@@ -103,8 +103,8 @@ def _draw(rng, n):
     return GAMMA, OBETA, DD, ro, tt, mom, fld
 
 
-def _check(a0s, mc, ok, mc_x, a0_x):
-    assert ok.sum() > 0.8 * ok.size, "too few certified samples to test the bound"
+def _check(a0s, mc, ok, mc_x, a0_x, min_certified=0.8):
+    assert ok.sum() > min_certified * ok.size, "too few certified samples to test the bound"
     for a0 in a0s:
         err = np.abs(a0[ok].astype(np.float64) / a0_x[ok] - 1.0)
         assert err.max() <= BOUND, err.max()
@@ -154,14 +154,7 @@ def test_fp32_storage_estimate_bound(mag, seed):
     a0s, mc, ok = estimate(*s, ro_f, tt_f, okin, f32(DD), f32(GAMMA), f32(OBETA), mag)
     mc_x, a0_x = exact(*[v.astype(np.float64) for v in s], ro, tt, DD, GAMMA, OBETA, mag)
     # the guard's rejects are evaluated exactly; the bound holds for the rest
-    ok_guarded = ok
-    assert ok_guarded.sum() > 0.4 * n
-    for a0 in a0s:
-        err = np.abs(a0[ok].astype(np.float64) / a0_x[ok] - 1.0)
-        assert err.max() <= BOUND, err.max()
-    sel = ok & (mc_x >= 2.0 ** -41)
-    err = np.abs(mc[sel].astype(np.float64) / mc_x[sel] - 1.0)
-    assert err.max() <= BOUND, err.max()
+    _check(a0s, mc, ok, mc_x, a0_x, min_certified=0.4)
 
 
 def test_guard_is_needed():
